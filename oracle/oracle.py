@@ -1,0 +1,183 @@
+"""ORACLE — CPU checker for the delay-and-sum path (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module.  The product package ``ustb_gb300`` never does.
+
+What is here:
+
+* ``das_f32``      — ctypes front end of ``das_port.c:oracle_das_f32``, the
+                     operation-for-operation single-precision restatement of the
+                     reference's das_c loop (+mex/source/das_c.cpp:355-409).
+* ``das_f64``      — the same formula in double precision ("FP64 oracle").
+* ``das_c_ref``    — the reference's own das_c (+mex/source/das_c.cpp) compiled
+                     unmodified by ``make -C oracle ref`` into oracle/_ref/.
+                     Available only where the reference sources were present at
+                     build time; returns None otherwise.
+* ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
+                     +postprocess/coherence_factor.m:100-135 and of the per-pixel
+                     term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
+
+Array convention: every array is given with its MATLAB logical shape
+(channel data [L, N, W, F], tables [P, W] / [P, N]) and is passed to C in
+column-major (Fortran) order, as MATLAB stores it.  Outputs come back as
+Fortran-ordered arrays of shape [P, N|1, W|1, F].
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PORT_SO = os.path.join(_HERE, "_build", "liboracle.so")
+_REF_SO = os.path.join(_HERE, "_ref", "libdas_c_ref.so")
+
+_port = None
+_ref = None
+
+_i64 = ctypes.c_int64
+_f32 = ctypes.c_float
+_f64 = ctypes.c_double
+_ptr = ctypes.c_void_p
+
+
+def build() -> None:
+    """Compile the C restatement (and the reference das_c when its source exists)."""
+    import subprocess
+
+    subprocess.check_call(["make", "-s", "-C", _HERE, "all"])
+    ref = os.environ.get("USTB_REFERENCE_ROOT", "/root/reference")
+    if os.path.isfile(os.path.join(ref, "+mex", "source", "das_c.cpp")):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"])
+
+
+def _load_port():
+    global _port
+    if _port is None:
+        if not os.path.isfile(_PORT_SO):
+            build()
+        lib = ctypes.CDLL(_PORT_SO)
+        lib.oracle_das_f32.restype = ctypes.c_int
+        lib.oracle_das_f32.argtypes = [_ptr, _i64, _i64, _i64, _i64, _f32, _f32, _ptr, _ptr, _ptr,
+                                       _ptr, _i64, _f32, ctypes.c_int32, _ptr, ctypes.c_int]
+        lib.oracle_das_f64.restype = ctypes.c_int
+        lib.oracle_das_f64.argtypes = [_ptr, _i64, _i64, _i64, _i64, _f64, _f64, _ptr, _ptr, _ptr,
+                                       _ptr, _i64, _f64, ctypes.c_int32, ctypes.c_int32, _ptr,
+                                       ctypes.c_int]
+        _port = lib
+    return _port
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        if not os.path.isfile(_REF_SO):
+            return None
+        lib = ctypes.CDLL(_REF_SO)
+        lib.das_c_ref_run.restype = ctypes.c_int
+        lib.das_c_ref_run.argtypes = [_ptr, _i64, _i64, _i64, _i64, _f32, _f32, _ptr, _ptr, _ptr,
+                                      _ptr, _i64, _f32, ctypes.c_int32, _ptr, ctypes.c_char_p,
+                                      ctypes.c_int]
+        _ref = lib
+    return _ref
+
+
+def have_reference() -> bool:
+    return _load_ref() is not None
+
+
+def _dims(ch):
+    s = list(ch.shape) + [1] * (4 - ch.ndim)
+    return tuple(int(v) for v in s[:4])
+
+
+def out_shape(P, N, W, F, dim):
+    return {0: (P, N, W, F), 1: (P, 1, W, F), 2: (P, N, 1, F), 3: (P, 1, 1, F)}[int(dim)]
+
+
+def _f(a, dtype):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def _threads(threads):
+    return int(threads) if threads else (os.cpu_count() or 1)
+
+
+def das_f32(ch, fs, t0, apo_tx, apo_rx, delay_tx, delay_rx, fd, dim, threads=None):
+    """Single-precision das_c restatement. ``ch`` complex64 [L,N,W,F]."""
+    L, N, W, F = _dims(ch)
+    c = _f(ch, np.complex64).reshape((L, N, W, F), order="F")
+    atx, arx = _f(apo_tx, np.float32), _f(apo_rx, np.float32)
+    dtx, drx = _f(delay_tx, np.float32), _f(delay_rx, np.float32)
+    P = atx.shape[0]
+    out = np.zeros(out_shape(P, N, W, F, dim), dtype=np.complex64, order="F")
+    rc = _load_port().oracle_das_f32(c.ctypes.data, L, N, W, F, float(np.float32(fs)),
+                                     float(np.float32(t0)), atx.ctypes.data, arx.ctypes.data,
+                                     dtx.ctypes.data, drx.ctypes.data, P, float(np.float32(fd)),
+                                     int(dim), out.ctypes.data, _threads(threads))
+    if rc != 0:
+        raise ValueError(f"oracle_das_f32 rejected its arguments (rc={rc})")
+    return out
+
+
+def das_f64(ch, fs, t0, apo_tx, apo_rx, delay_tx, delay_rx, fd, dim, edge_rule=0, threads=None):
+    """Double-precision restatement of the same formula. ``ch`` complex128 [L,N,W,F]."""
+    L, N, W, F = _dims(ch)
+    c = _f(ch, np.complex128).reshape((L, N, W, F), order="F")
+    atx, arx = _f(apo_tx, np.float64), _f(apo_rx, np.float64)
+    dtx, drx = _f(delay_tx, np.float64), _f(delay_rx, np.float64)
+    P = atx.shape[0]
+    out = np.zeros(out_shape(P, N, W, F, dim), dtype=np.complex128, order="F")
+    rc = _load_port().oracle_das_f64(c.ctypes.data, L, N, W, F, float(fs), float(t0),
+                                     atx.ctypes.data, arx.ctypes.data, dtx.ctypes.data,
+                                     drx.ctypes.data, P, float(fd), int(dim), int(edge_rule),
+                                     out.ctypes.data, _threads(threads))
+    if rc != 0:
+        raise ValueError(f"oracle_das_f64 rejected its arguments (rc={rc})")
+    return out
+
+
+def das_c_ref(ch, fs, t0, apo_tx, apo_rx, delay_tx, delay_rx, fd, dim) -> Optional[np.ndarray]:
+    """The reference's das_c itself (None when it was not built on this machine)."""
+    lib = _load_ref()
+    if lib is None:
+        return None
+    L, N, W, F = _dims(ch)
+    c = _f(ch, np.complex64).reshape((L, N, W, F), order="F")
+    atx, arx = _f(apo_tx, np.float32), _f(apo_rx, np.float32)
+    dtx, drx = _f(delay_tx, np.float32), _f(delay_rx, np.float32)
+    P = atx.shape[0]
+    out = np.zeros(out_shape(P, N, W, F, dim), dtype=np.complex64, order="F")
+    err = ctypes.create_string_buffer(512)
+    rc = lib.das_c_ref_run(c.ctypes.data, L, N, W, F, float(np.float32(fs)), float(np.float32(t0)),
+                           atx.ctypes.data, arx.ctypes.data, dtx.ctypes.data, drx.ctypes.data, P,
+                           float(np.float32(fd)), int(dim), out.ctypes.data, err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return out
+
+
+def coherence_factor(s, active_count):
+    """CF per +postprocess/coherence_factor.m:122-135 over axis 1 (channels).
+
+    ``s`` complex [P, N, ...]; ``active_count`` M per pixel.  Returns (CF, CF*sum).
+    """
+    s = np.asarray(s, dtype=np.complex128)
+    coh = s.sum(axis=1, keepdims=True)
+    inc = (np.abs(s) ** 2).sum(axis=1, keepdims=True)
+    M = np.asarray(active_count, dtype=np.float64).reshape((-1,) + (1,) * (s.ndim - 1))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        cf = (np.abs(coh) ** 2 / inc) * (1.0 / M)
+    cf[np.isnan(cf)] = 0.0
+    return cf, cf * coh
+
+
+def sdmas_value(s_real):
+    """Per-pixel simplified-DMAS term, simplified_delay_multiply_and_sum.m:143-146,
+    over axis 1 of a real array [P, N, ...]: ((sum sign*sqrt|s|)^2 - sum|s|)/2."""
+    s = np.asarray(s_real, dtype=np.float64)
+    root = (np.sign(s) * np.sqrt(np.abs(s))).sum(axis=1, keepdims=True)
+    absum = np.abs(s).sum(axis=1, keepdims=True)
+    return (root ** 2 - absum) / 2.0

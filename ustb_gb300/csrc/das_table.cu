@@ -1,0 +1,279 @@
+// Plain single-precision DAS on precomputed delay/apodization tables — the
+// drop-in for the reference's das_c (+mex/source/das_c.cpp:355-409).
+//
+// One thread per pixel.  For the summing modes each thread keeps FC frame
+// accumulators in registers and writes every output element exactly once, so
+// the output needs no clearing.  Per unit the arithmetic follows das_c step by
+// step in single precision, with the same roundings where they decide the
+// result: delay = fl(tx + rx), s = fl(fl(delay - t0) * fs), n0 = trunc(s),
+// b = s - floor(s), phase = fl(wd * delay).  Only the order of the final sums
+// and FMA contraction in the interpolation/rotation differ (a few ulp).
+//
+// Loop order: channels outer, waves inner (rx delay/apodization read once per
+// pixel-channel from HBM, the pixel's tx row re-read from L1), except for
+// dimension.receive, which keeps waves and sums channels (waves outer).
+#include "common.cuh"
+#include "phasor.cuh"
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr double kRefPi = 3.14159265359;  // the PI das_c uses for wd (das_c.cpp:33,243)
+
+struct TableArgs {
+    const void* ch;
+    int64_t L, N, W, F, P, LN, LNW;
+    float fs, t0, wd;
+    const float* apo_tx;
+    const float* apo_rx;
+    const float* d_tx;
+    const float* d_rx;
+    void* out;
+    int64_t rx_f, w_f, f_f;
+};
+
+template <bool CPLX, int FC>
+struct Acc {
+    float re[FC];
+    float im[FC];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int f = 0; f < FC; ++f) re[f] = im[f] = 0.f;
+    }
+};
+
+// Evaluate one (pixel, channel, wave) unit for frames [f0, f0+nf) and add it
+// into `acc` (which the caller zeroed for dimension.none).
+template <bool CPLX, int FC>
+__device__ __forceinline__ void unit(const TableArgs& A, int64_t n, int64_t w, int64_t f0, int nf,
+                                     float txd, float txa, float rxd, float rxa,
+                                     Acc<CPLX, FC>& acc) {
+    const float delay = __fadd_rn(txd, rxd);
+    const float apo = __fmul_rn(txa, rxa);
+    const float denay = __fmul_rn(__fsub_rn(delay, A.t0), A.fs);
+    const int n0 = __float2int_rz(denay);
+    if (!(n0 > 0 && (int64_t)n0 < A.L - 1)) return;
+    const float b = __fsub_rn(denay, floorf(denay));
+    const float a = __fsub_rn(1.0f, b);
+    const int64_t base = A.L * n + A.LN * w + n0 + f0 * A.LNW;
+    if (CPLX) {
+        float c, s;
+        ustb::expi_reduced(__fmul_rn(A.wd, delay), c, s);
+        const float wr = c * apo, wi = s * apo;
+        const float2* x = reinterpret_cast<const float2*>(A.ch) + base;
+#pragma unroll
+        for (int f = 0; f < FC; ++f) {
+            if (f < nf) {
+                const float2 x0 = __ldg(x + f * A.LNW);
+                const float2 x1 = __ldg(x + f * A.LNW + 1);
+                const float vr = fmaf(b, x1.x, a * x0.x);
+                const float vi = fmaf(b, x1.y, a * x0.y);
+                acc.re[f] = fmaf(wr, vr, fmaf(-wi, vi, acc.re[f]));
+                acc.im[f] = fmaf(wr, vi, fmaf(wi, vr, acc.im[f]));
+            }
+        }
+    } else {
+        const float* x = reinterpret_cast<const float*>(A.ch) + base;
+#pragma unroll
+        for (int f = 0; f < FC; ++f) {
+            if (f < nf) {
+                const float x0 = __ldg(x + f * A.LNW);
+                const float x1 = __ldg(x + f * A.LNW + 1);
+                acc.re[f] = fmaf(apo, fmaf(b, x1, a * x0), acc.re[f]);
+            }
+        }
+    }
+}
+
+template <bool CPLX, int FC>
+__device__ __forceinline__ void store(const TableArgs& A, int64_t idx, int64_t f0, int nf,
+                                      const Acc<CPLX, FC>& acc) {
+#pragma unroll
+    for (int f = 0; f < FC; ++f) {
+        if (f < nf) {
+            const int64_t o = idx + (f0 + f) * A.f_f;
+            if (CPLX)
+                reinterpret_cast<float2*>(A.out)[o] = make_float2(acc.re[f], acc.im[f]);
+            else
+                reinterpret_cast<float*>(A.out)[o] = acc.re[f];
+        }
+    }
+}
+
+template <int MODE, bool CPLX, int FC>
+__global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) {
+    const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (p >= A.P) return;
+    const int64_t P = A.P;
+    Acc<CPLX, FC> acc;
+    for (int64_t f0 = 0; f0 < A.F; f0 += FC) {
+        const int nf = (int)min((int64_t)FC, A.F - f0);
+        if (MODE == USTB_DIM_RECEIVE) {
+            for (int64_t w = 0; w < A.W; ++w) {
+                const float txd = __ldg(A.d_tx + P * w + p);
+                const float txa = __ldg(A.apo_tx + P * w + p);
+                acc.zero();
+                if (txa != 0.0f) {
+                    for (int64_t n = 0; n < A.N; ++n) {
+                        const float rxa = __ldg(A.apo_rx + P * n + p);
+                        if (rxa == 0.0f) continue;
+                        const float rxd = __ldg(A.d_rx + P * n + p);
+                        unit<CPLX, FC>(A, n, w, f0, nf, txd, txa, rxd, rxa, acc);
+                    }
+                }
+                store<CPLX, FC>(A, p + A.w_f * w, f0, nf, acc);
+            }
+        } else {
+            if (MODE == USTB_DIM_BOTH) acc.zero();
+            for (int64_t n = 0; n < A.N; ++n) {
+                const float rxa = __ldg(A.apo_rx + P * n + p);
+                const float rxd = __ldg(A.d_rx + P * n + p);
+                if (MODE == USTB_DIM_TRANSMIT) acc.zero();
+                if (rxa != 0.0f || MODE == USTB_DIM_NONE) {
+                    for (int64_t w = 0; w < A.W; ++w) {
+                        const float txa = __ldg(A.apo_tx + P * w + p);
+                        if (MODE == USTB_DIM_NONE) acc.zero();
+                        if (txa != 0.0f && rxa != 0.0f) {
+                            const float txd = __ldg(A.d_tx + P * w + p);
+                            unit<CPLX, FC>(A, n, w, f0, nf, txd, txa, rxd, rxa, acc);
+                        }
+                        if (MODE == USTB_DIM_NONE) store<CPLX, FC>(A, p + A.rx_f * n + A.w_f * w, f0, nf, acc);
+                    }
+                }
+                if (MODE == USTB_DIM_TRANSMIT) store<CPLX, FC>(A, p + A.rx_f * n, f0, nf, acc);
+            }
+            if (MODE == USTB_DIM_BOTH) store<CPLX, FC>(A, p, f0, nf, acc);
+        }
+    }
+}
+
+template <int MODE, bool CPLX>
+void launch_fc(const TableArgs& A, cudaStream_t s) {
+    const unsigned grid = (unsigned)((A.P + kThreads - 1) / kThreads);
+    if (A.F == 1)
+        das_table_kernel<MODE, CPLX, 1><<<grid, kThreads, 0, s>>>(A);
+    else if (A.F == 2)
+        das_table_kernel<MODE, CPLX, 2><<<grid, kThreads, 0, s>>>(A);
+    else
+        das_table_kernel<MODE, CPLX, 4><<<grid, kThreads, 0, s>>>(A);
+}
+
+template <bool CPLX>
+void launch_mode(int dim, const TableArgs& A, cudaStream_t s) {
+    switch (dim) {
+        case USTB_DIM_NONE: launch_fc<USTB_DIM_NONE, CPLX>(A, s); break;
+        case USTB_DIM_RECEIVE: launch_fc<USTB_DIM_RECEIVE, CPLX>(A, s); break;
+        case USTB_DIM_TRANSMIT: launch_fc<USTB_DIM_TRANSMIT, CPLX>(A, s); break;
+        default: launch_fc<USTB_DIM_BOTH, CPLX>(A, s); break;
+    }
+}
+
+int check_table_args(const void* ch, int32_t ch_complex, int64_t L, int64_t N, int64_t W, int64_t F,
+                     float fd, int32_t dim, const void* apo_tx, const void* apo_rx,
+                     const void* delay_tx, const void* delay_rx, int64_t P, const void* out) {
+    USTB_REQUIRE(dim >= 0 && dim <= 3, USTB_E_ARG,
+                 "Unknown sum mode %d. Available: 0 -> NONE, 1->RX, 2->TX, 3->BOTH", (int)dim);
+    USTB_REQUIRE(L >= 0 && N >= 0 && W >= 0 && F >= 0 && P >= 0, USTB_E_SHAPE,
+                 "negative size (L=%lld N=%lld W=%lld F=%lld P=%lld)", (long long)L, (long long)N,
+                 (long long)W, (long long)F, (long long)P);
+    USTB_REQUIRE(ch_complex == 0 || ch_complex == 1, USTB_E_ARG, "ch_complex must be 0 or 1");
+    USTB_REQUIRE(ch_complex || !(fabsf(fd) > 1e-6f), USTB_E_DTYPE,
+                 "The modulation frequency > 0 but the input data is real. Check inputs.");
+    USTB_REQUIRE(L <= INT32_MAX, USTB_E_SHAPE, "L=%lld exceeds the 32-bit sample index", (long long)L);
+    const bool empty_in = L == 0 || N == 0 || W == 0 || F == 0;
+    USTB_REQUIRE(empty_in || ch, USTB_E_ARG, "channel data pointer is NULL");
+    USTB_REQUIRE(P == 0 || (apo_tx && apo_rx && delay_tx && delay_rx), USTB_E_ARG,
+                 "a delay/apodization table pointer is NULL");
+    USTB_REQUIRE(out_elems(dim, P, N, W, F) == 0 || out, USTB_E_ARG, "output pointer is NULL");
+    return USTB_OK;
+}
+
+}  // namespace
+
+extern "C" int ustb_das_table_f32(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
+                                  int64_t W, int64_t F, float fs, float t0, const float* apo_tx,
+                                  const float* apo_rx, const float* delay_tx,
+                                  const float* delay_rx, int64_t P, float fd, int32_t dimension,
+                                  void* out, void* stream) {
+    ustb::clear_error();
+    int rc = check_table_args(ch, ch_complex, L, N, W, F, fd, dimension, apo_tx, apo_rx, delay_tx,
+                              delay_rx, P, out);
+    if (rc) return rc;
+    const int64_t n_out = out_elems(dimension, P, N, W, F);
+    if (n_out == 0) return USTB_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (L == 0 || N == 0 || W == 0) {
+        // nothing to sum: das_c returns its zero-initialised output
+        USTB_CUDA(cudaMemsetAsync(out, 0, (size_t)n_out * (ch_complex ? 8 : 4), s));
+        return USTB_OK;
+    }
+    TableArgs A;
+    A.ch = ch;
+    A.L = L; A.N = N; A.W = W; A.F = F; A.P = P;
+    A.LN = L * N; A.LNW = L * N * W;
+    A.fs = fs; A.t0 = t0;
+    A.wd = 0.0f;
+    if (fabsf(fd) > 1e-6f) A.wd = 2 * (float)kRefPi * fd;
+    A.apo_tx = apo_tx; A.apo_rx = apo_rx; A.d_tx = delay_tx; A.d_rx = delay_rx;
+    A.out = out;
+    const OutStrides os = out_strides(dimension, P, N, W);
+    A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
+    if (ch_complex)
+        launch_mode<true>(dimension, A, s);
+    else
+        launch_mode<false>(dimension, A, s);
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
+extern "C" int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
+                                       int64_t W, int64_t F, float fs, float t0,
+                                       const float* apo_tx, const float* apo_rx,
+                                       const float* delay_tx, const float* delay_rx, int64_t P,
+                                       float fd, int32_t dimension, void* out, int32_t device) {
+    ustb::clear_error();
+    int rc = check_table_args(ch, ch_complex, L, N, W, F, fd, dimension, apo_tx, apo_rx, delay_tx,
+                              delay_rx, P, out);
+    if (rc) return rc;
+    USTB_CUDA(cudaSetDevice(device));
+    const size_t el = ch_complex ? 8 : 4;
+    const size_t ch_bytes = (size_t)(L * N * W * F) * el;
+    const size_t tx_bytes = (size_t)(P * W) * 4, rx_bytes = (size_t)(P * N) * 4;
+    const size_t out_bytes = (size_t)out_elems(dimension, P, N, W, F) * el;
+    cudaStream_t s;
+    USTB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    char* buf = nullptr;
+    auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t total = align(ch_bytes) + 2 * align(tx_bytes) + 2 * align(rx_bytes) + align(out_bytes);
+    cudaError_t e = cudaMallocAsync((void**)&buf, total ? total : 256, s);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return ustb::cuda_fail(e, "cudaMallocAsync", __FILE__, __LINE__);
+    }
+    char* p = buf;
+    void* d_ch = p; p += align(ch_bytes);
+    float* d_atx = (float*)p; p += align(tx_bytes);
+    float* d_dtx = (float*)p; p += align(tx_bytes);
+    float* d_arx = (float*)p; p += align(rx_bytes);
+    float* d_drx = (float*)p; p += align(rx_bytes);
+    void* d_out = p;
+    rc = USTB_OK;
+    do {
+        if (ch_bytes && (e = cudaMemcpyAsync(d_ch, ch, ch_bytes, cudaMemcpyHostToDevice, s))) break;
+        if (tx_bytes && (e = cudaMemcpyAsync(d_atx, apo_tx, tx_bytes, cudaMemcpyHostToDevice, s))) break;
+        if (tx_bytes && (e = cudaMemcpyAsync(d_dtx, delay_tx, tx_bytes, cudaMemcpyHostToDevice, s))) break;
+        if (rx_bytes && (e = cudaMemcpyAsync(d_arx, apo_rx, rx_bytes, cudaMemcpyHostToDevice, s))) break;
+        if (rx_bytes && (e = cudaMemcpyAsync(d_drx, delay_rx, rx_bytes, cudaMemcpyHostToDevice, s))) break;
+        rc = ustb_das_table_f32(d_ch, ch_complex, L, N, W, F, fs, t0, d_atx, d_arx, d_dtx, d_drx, P,
+                                fd, dimension, d_out, s);
+        if (rc) break;
+        if (out_bytes && (e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s))) break;
+        e = cudaStreamSynchronize(s);
+    } while (0);
+    cudaFreeAsync(buf, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (rc) return rc;
+    if (e != cudaSuccess) return ustb::cuda_fail(e, "host-pointer DAS copy/sync", __FILE__, __LINE__);
+    return USTB_OK;
+}

@@ -1,0 +1,141 @@
+"""midprocess.das on the GB300 beamformer.
+
+``DAS`` keeps the properties of USTB's ``midprocess.das`` (+midprocess/das.m:49-63)
+and of the Python package's ``ustb.midprocess.DAS`` (python/src/ustb/midprocess/das.py:29-41),
+and its ``go()`` runs the same steps as das.m:77-317:
+
+1. transmit / receive apodization tables (das.m:91-100),
+2. receive and transmit delay tables (das.m:102-206), FP64 on the host, cast
+   to single as das.m does,
+3. channel data in single precision; RF data is made analytic with a Hilbert
+   transform along time (das.m:211-214) unless ``rf_mode = "real"``,
+4. the delay-and-sum itself through the C-ABI (``code = Code.gb300``), which
+   takes the place of mex.das_c (das.m:251-259),
+5. the per-pixel phase epilogue exp(-i 2 w0 r_ref / c) for IQ data (das.m:306-309),
+6. a ``BeamformedData`` on the scan (das.m:217-218, 312).
+
+The result tensor lives on the GPU; ``beamformed_data.data`` is a view with the
+MATLAB shape [P, N|1, W|1, F] (see ``kernels.to_matlab_order``).
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import geometry, kernels
+from .enums import Code, Dimension, Precision, SphericalTransmitDelayModel, Window
+from .geometry import Apodization
+from .uff import BeamformedData, ChannelData, Scan
+
+
+def channel_tensor(data, device) -> torch.Tensor:
+    """Channel data with MATLAB shape [L, N, W, F] (numpy or torch) -> ABI-layout tensor."""
+    if isinstance(data, np.ndarray):
+        a = data
+        while a.ndim < 4:
+            a = a[..., None]
+        dt = np.complex64 if np.iscomplexobj(a) else np.float32
+        t = torch.from_numpy(np.ascontiguousarray(a.astype(dt, copy=False).transpose(3, 2, 1, 0)))
+        return t.to(device)
+    t = data
+    while t.dim() < 4:
+        t = t.unsqueeze(-1)
+    if t.is_complex():
+        t = t.to(torch.complex64)
+    elif t.dtype not in (torch.float32,):
+        t = t.to(torch.float32)
+    return kernels.from_matlab_order(t.to(device))
+
+
+def hilbert_last(x: torch.Tensor) -> torch.Tensor:
+    """Analytic signal along the last dimension (the FFT method of MATLAB's hilbert)."""
+    L = x.shape[-1]
+    X = torch.fft.fft(x.to(torch.float32), dim=-1)
+    h = torch.zeros(L, dtype=torch.float32, device=x.device)
+    if L % 2 == 0:
+        h[0] = h[L // 2] = 1.0
+        h[1:L // 2] = 2.0
+    else:
+        h[0] = 1.0
+        h[1:(L + 1) // 2] = 2.0
+    return torch.fft.ifft(X * h, dim=-1).to(torch.complex64).contiguous()
+
+
+class DAS:
+    """Generalized delay-and-sum beamformer (midprocess.das) on GB300."""
+
+    def __init__(self):
+        self.channel_data: ChannelData = None
+        self.scan: Scan = None
+        self.dimension = Dimension.both
+        self.code = Code.gb300
+        self.gpu_id = 0
+        self.spherical_transmit_delay_model = SphericalTransmitDelayModel.hybrid
+        self.pw_margin = 1e-3
+        self.lens_delay = 0.0
+        self.blending_power = 0.5
+        self.receive_apodization = Apodization()
+        self.transmit_apodization = Apodization()
+        self.transmit_delay = None
+        self.receive_delay = None
+        self.elapsed_time = None
+        self.beamformed_data = None
+        # GB300 additions
+        self.precision = Precision.fp32
+        self.rf_mode = "analytic"  # "analytic" (das.m semantics) | "real" (real RF in, real out)
+
+    # -- tables ---------------------------------------------------------------
+    def tables(self):
+        """Single-precision (tx_apo, rx_apo, tx_delay, rx_delay) as das.m builds them."""
+        cd, scan = self.channel_data, self.scan
+        tx_apo = self.transmit_apodization.wave_apodization(cd.sequence, scan).astype(np.float32)
+        rx_apo = self.receive_apodization.aperture_apodization(cd.probe, scan).astype(np.float32)
+        rx_delay = geometry.receive_delay(cd.probe, scan, cd.sound_speed,
+                                          self.lens_delay).astype(np.float32)
+        tx_delay = geometry.transmit_delay(
+            cd.sequence, scan, self.spherical_transmit_delay_model, self.pw_margin,
+            self.blending_power, self.transmit_apodization.f_number).astype(np.float32)
+        self.receive_delay = rx_delay
+        self.transmit_delay = tx_delay
+        return tx_apo, rx_apo, tx_delay, rx_delay
+
+    def pixel_phase(self) -> np.ndarray:
+        """exp(-1j*2*w0*reference_distance/c) per pixel, in double (das.m:307-309)."""
+        cd = self.channel_data
+        w0 = 2 * math.pi * float(np.float32(cd.modulation_frequency))
+        return np.exp(-1j * 2 * w0 * np.asarray(self.scan.reference_distance, np.float64)
+                      * np.ones(self.scan.N_pixels) / cd.sound_speed)
+
+    # -- go -------------------------------------------------------------------
+    def go(self) -> BeamformedData:
+        if Code(int(self.code)) != Code.gb300:
+            raise ValueError("this beamformer implements code.gb300 only")
+        cd, scan = self.channel_data, self.scan
+        dev = torch.device("cuda", int(self.gpu_id))
+        fs = float(np.float32(cd.sampling_frequency))
+        t0 = float(np.float32(cd.initial_time))
+        fd = float(np.float32(cd.modulation_frequency))
+        w0 = 2 * math.pi * fd
+        tx_apo, rx_apo, tx_delay, rx_delay = self.tables()
+        ch = channel_tensor(cd.data, dev)
+        if abs(w0) < np.finfo(np.float64).eps:
+            if ch.is_complex():
+                pass
+            elif self.rf_mode == "analytic":
+                ch = hilbert_last(ch)
+        elif not ch.is_complex():
+            raise ValueError("The modulation frequency > 0 but the input data is real. Check inputs.")
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
+        t_start = time.perf_counter()
+        out = kernels.das_table_f32(ch, fs, t0, T(tx_apo), T(rx_apo), T(tx_delay), T(rx_delay),
+                                    fd, self.dimension)
+        if abs(w0) > np.finfo(np.float64).eps:
+            ph = torch.from_numpy(self.pixel_phase().astype(np.complex64)).to(dev)
+            kernels.apply_pixel_phase(out, ph)
+        torch.cuda.synchronize(dev)
+        self.elapsed_time = time.perf_counter() - t_start
+        self.beamformed_data = BeamformedData(scan, kernels.to_matlab_order(out))
+        return self.beamformed_data
