@@ -99,7 +99,7 @@ def test_table_kernel_deterministic(golden_dir, cuda_dev):
     c = _case(golden_dir, "iq_small")
     a = run_table(c, 3, cuda_dev)
     b = run_table(c, 3, cuda_dev)
-    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
 
 
 def test_host_entry_point(golden_dir, cuda_dev):
