@@ -99,6 +99,119 @@ int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64_t L, int64
  */
 int ustb_apply_pixel_phase(void* data, int64_t P, int64_t rest, const void* phase, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Fast path: reduced-precision channel storage, on-the-fly geometry         */
+/* ------------------------------------------------------------------------ */
+
+/* Channel-data storage on the device (arithmetic is always single precision). */
+enum { USTB_STORE_F32 = 0, USTB_STORE_F16 = 1, USTB_STORE_BF16 = 2 };
+
+/* Source types of ustb_convert_channels. */
+enum { USTB_SRC_F32 = 0, USTB_SRC_I16 = 1, USTB_SRC_F16 = 2 };
+
+/* Transmit-delay models of ustb_wave.kind (+midprocess/das.m:110-206). */
+enum {
+    USTB_WAVE_PLANE = 0,     /* tau = (dir . x)/c - delay                          das.m:193 */
+    USTB_WAVE_SPHERICAL = 1, /* tau = (sigma*|x - src| + offset)/c - delay,
+                                sigma = -1 where z < src_z                 das.m:120-132 */
+    USTB_WAVE_ZERO = 2,      /* tau = -delay (photoacoustic)                    das.m:196-197 */
+    USTB_WAVE_TABLE = 3      /* tau read from ustb_das_geometry.tx_delay_table [P,W] */
+};
+
+/* One transmit event.  48 bytes, 4-byte aligned members. */
+typedef struct {
+    int32_t kind;        /* USTB_WAVE_* */
+    float dir[3];        /* plane: (sin az cos el, sin el, cos az cos el) */
+    float src[3];        /* spherical: virtual source position, m */
+    float offset;        /* spherical: -|distance| (diverging) or +distance (focused), m */
+    float sound_speed;   /* wave.sound_speed, m/s */
+    float delay;         /* wave.delay, s */
+    float apodization;   /* constant transmit apodization (when tx_apo_table is NULL) */
+    float reserved;
+} ustb_wave;
+
+/* Receive window ids (same values as +uff/window.m). */
+enum {
+    USTB_WIN_NONE = 0, USTB_WIN_BOXCAR = 1, USTB_WIN_HANNING = 2, USTB_WIN_HAMMING = 3,
+    USTB_WIN_TUKEY25 = 4, USTB_WIN_TUKEY50 = 5, USTB_WIN_TUKEY75 = 6, USTB_WIN_TRIANGLE = 9
+};
+
+/* Pixels per tile of the fast path (one CTA). */
+#define USTB_TILE_PIXELS 256
+
+/*
+ * Geometry of one beamforming request.  All pointers are device pointers.
+ * Pixels are processed in tiles of USTB_TILE_PIXELS: tile_pixels[t][j] is the
+ * pixel index handled by lane j of tile t (-1 = idle lane; lane 0 of every tile
+ * must be live).  Compact tiles keep each channel/wave sample window short.
+ */
+typedef struct {
+    int64_t n_elements;
+    const float* element_xyz;    /* [N][3] m */
+    int64_t n_pixels;
+    const float* pixel_xyz;      /* [P][3] m */
+    int64_t n_tiles;
+    const int32_t* tile_pixels;  /* [n_tiles][USTB_TILE_PIXELS] */
+    int64_t n_waves;
+    const ustb_wave* waves;      /* [W] */
+    const float* tx_delay_table; /* [P,W] s for USTB_WAVE_TABLE waves, else NULL */
+    const float* tx_apo_table;   /* [P,W] or NULL (then ustb_wave.apodization) */
+    const float* rx_apo_table;   /* [P,N] or NULL (then the receive window below) */
+    const float* pixel_phase;    /* [P] interleaved complex factor applied to every output, or NULL */
+    float fs, t0, fd, sound_speed, lens_delay;
+    /* receive apodization, +uff/apodization.m:323-468 (flat probe, no tilt) */
+    int32_t rx_window;           /* USTB_WIN_* */
+    float rx_f_number[2];
+    float rx_min_aperture[2];
+    float rx_max_aperture[2];
+    int32_t rx_use_origin;       /* 0: aperture centred under each pixel; 1: at rx_origin (sector scans) */
+    float rx_origin[3];
+    float cf_threshold;          /* coherence factor: elements with rx apodization > this count in M */
+} ustb_das_geometry;
+
+/* Outputs of ustb_das_fast (device pointers; unused ones NULL). */
+typedef struct {
+    void* cube;       /* [P, N|1, W|1, F] per `dimension`: complex single (or real single for RF) */
+    void* das;        /* epilogue: [P, F] complex, the channel sum (the dimension.both image) */
+    float* cf;        /* epilogue: [P, F] coherence factor |sum s|^2 / (M * sum |s|^2) */
+    void* cf_image;   /* epilogue: [P, F] complex, cf * sum s */
+    float* sdmas;     /* epilogue: [P, F] ((sum sign(re s) sqrt|re s|)^2 - sum |re s|)/2 */
+} ustb_das_outputs;
+
+/* ustb_das_fast flag bits (written to *flags, device memory). */
+#define USTB_FLAG_WINDOW_OVERFLOW 1u
+
+/*
+ * Delay-and-sum with channel data stored as single, half or bfloat16 and the
+ * delays, apodization and phase formed on the fly in single precision (the
+ * reference forms them as tables in MATLAB: +midprocess/das.m:91-209, then calls
+ * das_c: +mex/source/das_c.cpp:355-409).  Same formula as das_c — validity
+ * 0 < n0 < L-1, linear interpolation, exp(i 2 pi fd tau) rotation, tx x rx
+ * apodization, summation per `dimension` — with the phase factored per
+ * pixel-wave and pixel-channel.  Results are checked against a double-precision
+ * oracle of that formula, not bit-for-bit against das_c.
+ *
+ * ch: [L,N,W,F] of the given storage; complex (interleaved) when is_complex,
+ * else real RF (fd must be 0; outputs are then real).
+ * epilogue = 1 (dimension.transmit, complex only) also produces the coherence
+ * factor (+postprocess/coherence_factor.m:100-135, over channels) and the
+ * per-pixel simplified-DMAS value (+postprocess/simplified_delay_multiply_and_sum.m:140-148)
+ * without writing the channel cube (out->cube may be NULL).
+ * flags: device uint32, cleared by the call; USTB_FLAG_WINDOW_OVERFLOW means a
+ * tile was too large for its sample windows (re-plan with smaller tiles).
+ */
+int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
+                  int64_t W, int64_t F, const ustb_das_geometry* geometry, int32_t dimension,
+                  int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream);
+
+/*
+ * Convert channel data to a device storage type: count scalars from `src`
+ * (USTB_SRC_*) times `scale` into `dst` (USTB_STORE_*), e.g. int16 I/Q scanner
+ * samples or complex64 into half.  Device pointers; stream-ordered.
+ */
+int ustb_convert_channels(const void* src, int32_t src_type, void* dst, int32_t dst_type,
+                          int64_t count, float scale, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

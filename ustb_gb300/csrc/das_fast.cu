@@ -1,0 +1,699 @@
+// Fast delay-and-sum: reduced-precision channel storage, geometry formed on the
+// fly, factored phase, sample windows staged in shared memory.
+//
+// Same formula as the reference's das_c (+mex/source/das_c.cpp:355-409), with
+// the tables das.m builds in MATLAB (+midprocess/das.m:91-209) computed per
+// pixel-channel and pixel-wave in registers:
+//
+//   y = sum_w sum_n  A_w(p) * B_n(p) * lerp(x_{n,w}, s_tx(p,w) + s_rx(p,n))
+//   A_w = apo_tx * exp(i 2 pi fd tau_tx),  B_n = apo_rx * exp(i 2 pi fd tau_rx)
+//
+// One CTA beamforms a tile of 256 pixels (one per thread) for one frame.  The
+// (channel, wave) pairs are processed in stages of CG x KW; for each pair the
+// tile needs a short window of samples starting at i0 = base_n + base_w, where
+// base_n / base_w are integer lower bounds of the tile's receive / transmit
+// delays (in samples) derived from the tile's bounding box.  The window is
+// staged as interpolation entries {x_i, x_{i+1} - x_i} in FP32 with das_c's
+// validity rule (0 < i < L-1) folded in as zero entries, so a unit costs:
+//   s = s_tx_loc + s_rx_loc; j = floor(s); b = s - j; e = slot[j];
+//   v = e.x + b*e.d;  acc += weight * v.
+// Delays relative to the tile bases stay below 64 samples, so j and b keep
+// full sub-sample precision in FP32.
+//
+// Loop orders: waves outer / channels inner for dimension.both and .receive
+// (rx weight per unit, tx weight once per wave chunk); channels outer / waves
+// inner for .transmit and .none (tx weight per unit).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+#include "phasor.cuh"
+
+namespace {
+
+constexpr int kTile = USTB_TILE_PIXELS;
+constexpr int kSlot = 128;                      // entries per (channel, wave) window
+constexpr float kHalf = (float)(kSlot / 2 - 1);  // max relative delay of each component
+constexpr float kMagic = 8388608.0f;            // 2^23: floor via round-toward-zero add
+constexpr int kMagicBits = 0x4B000000;
+
+struct Params {
+    const void* ch;
+    int64_t L, N, W, F, P;
+    const float* el;
+    const float* px;
+    const int32_t* tiles;
+    const ustb_wave* waves;
+    const float* tx_delay_tab;
+    const float* tx_apo_tab;
+    const float* rx_apo_tab;
+    const float2* pix_phase;
+    float fs, t0, fd, inv_c, lens;
+    int rx_window;
+    float fnx, fny, minx, miny, maxx, maxy;
+    int rx_origin;
+    float ox, oy, oz;
+    float cf_thr;
+    void* cube;
+    float2* o_das;
+    float* o_cf;
+    float2* o_cfimg;
+    float* o_sdmas;
+    int64_t rx_f, w_f, f_f;
+    uint32_t* flags;
+};
+
+// ---------------------------------------------------------------------------
+// sample loads
+// ---------------------------------------------------------------------------
+template <int ST, bool CPLX>
+struct Sample;
+
+template <>
+struct Sample<USTB_STORE_F32, true> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return __ldg(reinterpret_cast<const float2*>(base) + i);
+    }
+};
+template <>
+struct Sample<USTB_STORE_F16, true> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return __half22float2(__ldg(reinterpret_cast<const __half2*>(base) + i));
+    }
+};
+template <>
+struct Sample<USTB_STORE_BF16, true> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(base) + i));
+    }
+};
+template <>
+struct Sample<USTB_STORE_F32, false> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return make_float2(__ldg(reinterpret_cast<const float*>(base) + i), 0.f);
+    }
+};
+template <>
+struct Sample<USTB_STORE_F16, false> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return make_float2(__half2float(__ldg(reinterpret_cast<const __half*>(base) + i)), 0.f);
+    }
+};
+template <>
+struct Sample<USTB_STORE_BF16, false> {
+    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
+        return make_float2(__bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(base) + i)), 0.f);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// apodization windows, +uff/apodization.m:172-223 (0 beyond ratio 1/2)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float tukey(float r, float roll) {
+    const float lo = 0.5f * (1.f - roll);
+    if (r <= lo) return 1.f;
+    if (r > lo && r < 0.5f) return 0.5f * (1.f + __cosf(6.283185307179586f / roll * (r - roll * 0.5f - 0.5f)));
+    return 0.f;
+}
+
+__device__ __forceinline__ float window(int win, float r) {
+    switch (win) {
+        case USTB_WIN_NONE: return 1.f;
+        case USTB_WIN_BOXCAR: return r <= 0.5f ? 1.f : 0.f;
+        case USTB_WIN_HANNING: return r <= 0.5f ? 0.5f + 0.5f * __cosf(6.283185307179586f * r) : 0.f;
+        case USTB_WIN_HAMMING: return r <= 0.5f ? 0.53836f + 0.46164f * __cosf(6.283185307179586f * r) : 0.f;
+        case USTB_WIN_TUKEY25: return tukey(r, 0.25f);
+        case USTB_WIN_TUKEY50: return tukey(r, 0.50f);
+        case USTB_WIN_TUKEY75: return tukey(r, 0.75f);
+        case USTB_WIN_TRIANGLE: return r <= 0.5f ? 1.f - 2.f * r : 0.f;
+        default: return 0.f;
+    }
+}
+
+__device__ __forceinline__ float msign(float v) { return (float)((v > 0.f) - (v < 0.f)); }
+
+// min/max aperture clamps of apodization.m:452-462 (MATLAB sign(0) = 0)
+__device__ __forceinline__ float clamp_ap(float z, float fnum, float minap, float maxap) {
+    const float a = fabsf(z);
+    const float lo = minap * fnum, hi = maxap * fnum;
+    float r = z;
+    if (a <= lo) r = msign(z) * lo;
+    if (a >= hi) r = msign(z) * hi;
+    return r;
+}
+
+__device__ __forceinline__ float rx_apodization(const Params& A, float ex, float ey, float ez, float px,
+                                                float py, float pz) {
+    if (A.rx_window == USTB_WIN_NONE) return 1.f;
+    float xd, yd, zd;
+    if (A.rx_origin) {
+        xd = ex - A.ox;
+        yd = ey - A.oy;
+        const float qx = px - A.ox, qy = py - A.oy, qz = pz - A.oz;
+        zd = sqrtf(qx * qx + qy * qy + qz * qz);
+    } else {
+        xd = px - ex;
+        yd = py - ey;
+        zd = pz - ez;
+    }
+    const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
+    const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
+    const float rt = fabsf(A.fnx * (xd / zx));
+    const float rp = fabsf(A.fny * (yd / zy));
+    return window(A.rx_window, rt) * window(A.rx_window, rp);
+}
+
+// exp(i 2 pi fd tau) from the phase in cycles
+__device__ __forceinline__ float2 phasor_cycles(float cyc) {
+    const float k = rintf(cyc);
+    const float fr = cyc - k;  // exact for |cyc| < 2^22
+    float s, c;
+    __sincosf(6.283185307179586f * fr, &s, &c);
+    return make_float2(c, s);
+}
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ void dist_range(const Box& b, float x, float y, float z, float& dmin, float& dmax) {
+    const float q[3] = {x, y, z};
+    float n2 = 0.f, f2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float dl = b.lo[i] - q[i], dh = q[i] - b.hi[i];
+        const float dn = fmaxf(0.f, fmaxf(dl, dh));
+        const float df = fmaxf(fabsf(q[i] - b.lo[i]), fabsf(q[i] - b.hi[i]));
+        n2 += dn * dn;
+        f2 += df * df;
+    }
+    dmin = sqrtf(n2);
+    dmax = sqrtf(f2);
+}
+
+// transmit delay (s) of one wave at one pixel
+__device__ __forceinline__ float tx_tau(const Params& A, const ustb_wave& wv, int64_t w, int64_t p,
+                                        float px, float py, float pz) {
+    switch (wv.kind) {
+        case USTB_WAVE_PLANE:
+            return (px * wv.dir[0] + py * wv.dir[1] + pz * wv.dir[2]) / wv.sound_speed - wv.delay;
+        case USTB_WAVE_SPHERICAL: {
+            const float dx = px - wv.src[0], dy = py - wv.src[1], dz = pz - wv.src[2];
+            const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float sg = pz < wv.src[2] ? -1.f : 1.f;
+            return (sg * d + wv.offset) / wv.sound_speed - wv.delay;
+        }
+        case USTB_WAVE_TABLE: return __ldg(A.tx_delay_tab + w * A.P + p);
+        default: return -wv.delay;
+    }
+}
+
+// lower / upper bound of a wave's transmit delay (s) over the tile box
+__device__ __forceinline__ void tx_tau_range(const ustb_wave& wv, const Box& b, float& lo, float& hi) {
+    switch (wv.kind) {
+        case USTB_WAVE_PLANE: {
+            float mn = 0.f, mx = 0.f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float u = wv.dir[i] * b.lo[i], v = wv.dir[i] * b.hi[i];
+                mn += fminf(u, v);
+                mx += fmaxf(u, v);
+            }
+            lo = mn / wv.sound_speed - wv.delay;
+            hi = mx / wv.sound_speed - wv.delay;
+            return;
+        }
+        case USTB_WAVE_SPHERICAL: {
+            float dmin, dmax;
+            dist_range(b, wv.src[0], wv.src[1], wv.src[2], dmin, dmax);
+            float vlo, vhi;
+            if (b.lo[2] >= wv.src[2]) { vlo = dmin; vhi = dmax; }
+            else if (b.hi[2] < wv.src[2]) { vlo = -dmax; vhi = -dmin; }
+            else { vlo = -dmax; vhi = dmax; }
+            lo = (vlo + wv.offset) / wv.sound_speed - wv.delay;
+            hi = (vhi + wv.offset) / wv.sound_speed - wv.delay;
+            return;
+        }
+        default:
+            lo = hi = -wv.delay;
+            return;
+    }
+}
+
+// block-wide min/max of one float (all threads call; result broadcast)
+__device__ __forceinline__ float2 block_minmax(float vmin, float vmax, float2* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) red[warp] = make_float2(vmin, vmax);
+    __syncthreads();
+    float2 r = red[0];
+#pragma unroll
+    for (int i = 1; i < kTile / 32; ++i) {
+        r.x = fminf(r.x, red[i].x);
+        r.y = fmaxf(r.y, red[i].y);
+    }
+    return r;
+}
+
+template <bool CPLX>
+struct EntryT { using type = float4; };
+template <>
+struct EntryT<false> { using type = float2; };
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <int MODE, bool CPLX, int ST, bool EPI>
+__global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
+    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
+    constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
+    constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
+    constexpr int NS = CG * KW;
+    using Entry = typename EntryT<CPLX>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Entry* slots = reinterpret_cast<Entry*>(smem_raw);
+    __shared__ int s_base_n[CG], s_base_w[KW];
+    __shared__ int s_len_n[CG], s_len_w[KW];  // ceil(upper bound - base) per component
+    __shared__ int s_act_n[CG], s_act_w[KW];
+    __shared__ float2 s_red[kTile / 32];
+
+    const int tid = threadIdx.x;
+    const int64_t f = blockIdx.y;
+    const int32_t* tl = A.tiles + (int64_t)blockIdx.x * kTile;
+    const int32_t p_own = __ldg(tl + tid);
+    const bool live = p_own >= 0;
+    const int64_t p = live ? p_own : __ldg(tl);
+    const float px = __ldg(A.px + 3 * p), py = __ldg(A.px + 3 * p + 1), pz = __ldg(A.px + 3 * p + 2);
+
+    // tile bounding box
+    Box box;
+    {
+        const float big = 3.4e38f;
+        float2 r;
+        r = block_minmax(live ? px : big, live ? px : -big, s_red);
+        box.lo[0] = r.x; box.hi[0] = r.y;
+        r = block_minmax(live ? py : big, live ? py : -big, s_red);
+        box.lo[1] = r.x; box.hi[1] = r.y;
+        r = block_minmax(live ? pz : big, live ? pz : -big, s_red);
+        box.lo[2] = r.x; box.hi[2] = r.y;
+    }
+    const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
+    const float fd_c = A.fd * A.inv_c;  // cycles per metre
+
+    const int64_t L = A.L, N = A.N, W = A.W, P = A.P;
+    const char* chf = reinterpret_cast<const char*>(A.ch);
+    const int64_t esz = CPLX ? (ST == USTB_STORE_F32 ? 8 : 4) : (ST == USTB_STORE_F32 ? 4 : 2);
+    const int64_t frame_off = f * W * N * L;
+
+    // per-thread state
+    float srx[CG];
+    float2 B[CG];
+    float rxapo[CG];
+    float stx[KW];
+    float2 Aw[KW];
+    float accr[ORDER_A ? KW : CG], acci[ORDER_A ? KW : CG];
+    float2 Y = make_float2(0.f, 0.f);  // dimension.both
+    // epilogue accumulators
+    float2 eS = make_float2(0.f, 0.f);
+    float eI = 0.f, eM = 0.f, eR = 0.f, eQ = 0.f;
+
+    auto setup_rx = [&](int64_t n0, int cg) {
+#pragma unroll
+        for (int c = 0; c < CG; ++c) {
+            const int64_t n = n0 + c;
+            float s = 0.f, apo = 0.f;
+            float2 b = make_float2(0.f, 0.f);
+            if (c < cg) {
+                const float ex = __ldg(A.el + 3 * n), ey = __ldg(A.el + 3 * n + 1), ez = __ldg(A.el + 3 * n + 2);
+                const float dx = px - ex, dy = py - ey, dz = pz - ez;
+                const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+                const float tau = r * A.inv_c + A.lens;
+                s = tau * A.fs;
+                apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
+                if (!live) apo = 0.f;
+                if (CPLX) {
+                    const float2 e = phasor_cycles(r * fd_c + A.lens * A.fd);
+                    b = make_float2(apo * e.x, apo * e.y);
+                } else {
+                    b = make_float2(apo, 0.f);
+                }
+                if (tid == 0) {
+                    float dmin, dmax;
+                    dist_range(box, ex, ey, ez, dmin, dmax);
+                    const float lo = (dmin * A.inv_c + A.lens) * A.fs, hi = (dmax * A.inv_c + A.lens) * A.fs;
+                    const float base = floorf(lo) - 1.f;
+                    if (!(hi - base <= kHalf - 2.f) || !(fabsf(base) < 1.0e9f)) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
+                    s_base_n[c] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                    s_len_n[c] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
+                }
+            }
+            srx[c] = s;
+            B[c] = b;
+            rxapo[c] = apo;
+            const int any = __syncthreads_or(apo != 0.f);
+            if (tid == 0) s_act_n[c] = (c < cg) && any;
+        }
+    };
+
+    auto setup_tx = [&](int64_t w0, int kw) {
+        // table-driven delays need the tile's actual range
+#pragma unroll
+        for (int k = 0; k < KW; ++k) {
+            const int64_t w = w0 + k;
+            float s = 0.f, apo = 0.f;
+            float2 a = make_float2(0.f, 0.f);
+            if (k < kw) {
+                const ustb_wave wv = A.waves[w];
+                const float tau = tx_tau(A, wv, w, p, px, py, pz);
+                s = (tau - A.t0) * A.fs;
+                apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + w * P + p) : wv.apodization;
+                if (!live) apo = 0.f;
+                if (CPLX) {
+                    const float2 e = phasor_cycles(tau * A.fd);
+                    a = make_float2(apo * e.x, apo * e.y);
+                } else {
+                    a = make_float2(apo, 0.f);
+                }
+                float lo, hi;
+                if (wv.kind == USTB_WAVE_TABLE) {
+                    const float2 r = block_minmax(live ? s : 3.4e38f, live ? s : -3.4e38f, s_red);
+                    lo = r.x; hi = r.y;
+                } else {
+                    tx_tau_range(wv, box, lo, hi);
+                    lo = (lo - A.t0) * A.fs;
+                    hi = (hi - A.t0) * A.fs;
+                }
+                if (tid == 0) {
+                    const float base = floorf(lo) - 1.f;
+                    if (!(hi - base <= kHalf - 2.f) || !(fabsf(base) < 1.0e9f)) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
+                    s_base_w[k] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                    s_len_w[k] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
+                }
+            }
+            stx[k] = s;
+            Aw[k] = a;
+            const int any = __syncthreads_or(apo != 0.f);
+            if (tid == 0) s_act_w[k] = (k < kw) && any;
+        }
+    };
+
+    // convert absolute delays to window-relative, clamped into [0, kHalf]
+    // (NaN and out-of-window values end up inside the slot; overflow is flagged)
+    auto localise_rx = [&]() {
+        __syncthreads();  // s_base_n visible
+#pragma unroll
+        for (int c = 0; c < CG; ++c) srx[c] = fminf(fmaxf(srx[c] - (float)s_base_n[c], 0.f), kHalf);
+    };
+    auto localise_tx = [&]() {
+        __syncthreads();  // s_base_w visible
+#pragma unroll
+        for (int k = 0; k < KW; ++k) stx[k] = fminf(fmaxf(stx[k] - (float)s_base_w[k], 0.f), kHalf);
+    };
+
+    // Stage the windows of (channel group n0, wave chunk w0): one warp per slot,
+    // only the entries the tile can reach (len = spans + margin, <= kSlot).
+    auto stage_fill = [&](int64_t n0, int64_t w0) {
+        __syncthreads();  // previous stage consumed
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int slot = warp; slot < NS; slot += kTile / 32) {
+            const int c = slot / KW, k = slot - c * KW;
+            if (!(s_act_n[c] && s_act_w[k])) continue;
+            const int len = min(kSlot, s_len_n[c] + s_len_w[k] + 3);
+            const int64_t i0 = (int64_t)s_base_n[c] + s_base_w[k];
+            const int64_t tb = frame_off + ((w0 + k) * N + (n0 + c)) * L;
+            Entry* dst = slots + slot * kSlot;
+            for (int j = lane; j < len; j += 32) {
+                const int64_t i = i0 + j;
+                Entry v;
+                if constexpr (CPLX) v = make_float4(0.f, 0.f, 0.f, 0.f);
+                else v = make_float2(0.f, 0.f);
+                if (i >= 1 && i <= L - 2) {
+                    const float2 x0 = Sample<ST, CPLX>::load(chf, tb + i);
+                    const float2 x1 = Sample<ST, CPLX>::load(chf, tb + i + 1);
+                    if constexpr (CPLX) v = make_float4(x0.x, x0.y, x1.x - x0.x, x1.y - x0.y);
+                    else v = make_float2(x0.x, x1.x - x0.x);
+                }
+                dst[j] = v;
+            }
+        }
+        __syncthreads();
+    };
+
+    // one unit: interpolated sample of slot (c, k) at relative delay s
+    auto interp = [&](int c, int k, float s) -> float2 {
+        const float t = __fadd_rz(s, kMagic);
+        const int j = __float_as_int(t) - kMagicBits;
+        const float b = s - (t - kMagic);
+        const Entry e = slots[(c * KW + k) * kSlot + j];
+        if constexpr (CPLX) return make_float2(fmaf(b, e.z, e.x), fmaf(b, e.w, e.y));
+        else return make_float2(fmaf(b, e.y, e.x), 0.f);
+    };
+
+    (void)esz;
+    if constexpr (ORDER_A) {
+        for (int64_t w0 = 0; w0 < W; w0 += KW) {
+            const int kw = (int)min((int64_t)KW, W - w0);
+            setup_tx(w0, kw);
+            localise_tx();
+#pragma unroll
+            for (int k = 0; k < KW; ++k) accr[k] = acci[k] = 0.f;
+            for (int64_t n0 = 0; n0 < N; n0 += CG) {
+                const int cg = (int)min((int64_t)CG, N - n0);
+                setup_rx(n0, cg);
+                localise_rx();
+                stage_fill(n0, w0);
+#pragma unroll
+                for (int c = 0; c < CG; ++c) {
+                    if (!s_act_n[c]) continue;
+                    const float2 b = B[c];
+#pragma unroll
+                    for (int k = 0; k < KW; ++k) {
+                        if (!s_act_w[k]) continue;
+                        const float2 v = interp(c, k, stx[k] + srx[c]);
+                        if constexpr (CPLX) {
+                            accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
+                            acci[k] = fmaf(b.x, v.y, fmaf(b.y, v.x, acci[k]));
+                        } else {
+                            accr[k] = fmaf(b.x, v.x, accr[k]);
+                        }
+                    }
+                }
+            }
+            // fold the wave chunk
+#pragma unroll
+            for (int k = 0; k < KW; ++k) {
+                if (k >= kw) continue;
+                float2 y;
+                if constexpr (CPLX) y = cmul(Aw[k], make_float2(accr[k], acci[k]));
+                else y = make_float2(Aw[k].x * accr[k], 0.f);
+                if (MODE == USTB_DIM_BOTH) {
+                    Y.x += y.x;
+                    Y.y += y.y;
+                } else if (live && A.cube) {
+                    const int64_t o = p + A.w_f * (w0 + k) + A.f_f * f;
+                    if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = cmul(y, ph);
+                    else reinterpret_cast<float*>(A.cube)[o] = y.x;
+                }
+            }
+        }
+        if (MODE == USTB_DIM_BOTH && live && A.cube) {
+            const int64_t o = p + A.f_f * f;
+            if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = cmul(Y, ph);
+            else reinterpret_cast<float*>(A.cube)[o] = Y.x;
+        }
+    } else {
+        for (int64_t n0 = 0; n0 < N; n0 += CG) {
+            const int cg = (int)min((int64_t)CG, N - n0);
+            setup_rx(n0, cg);
+            localise_rx();
+#pragma unroll
+            for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
+            for (int64_t w0 = 0; w0 < W; w0 += KW) {
+                const int kw = (int)min((int64_t)KW, W - w0);
+                setup_tx(w0, kw);
+                localise_tx();
+                stage_fill(n0, w0);
+#pragma unroll
+                for (int c = 0; c < CG; ++c) {
+                    if (!s_act_n[c]) continue;
+#pragma unroll
+                    for (int k = 0; k < KW; ++k) {
+                        if (!s_act_w[k]) continue;
+                        const float2 v = interp(c, k, stx[k] + srx[c]);
+                        if (MODE == USTB_DIM_NONE) {
+                            if (live && A.cube) {
+                                const int64_t o = p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f;
+                                if constexpr (CPLX)
+                                    reinterpret_cast<float2*>(A.cube)[o] = cmul(cmul(cmul(Aw[k], B[c]), v), ph);
+                                else
+                                    reinterpret_cast<float*>(A.cube)[o] = Aw[k].x * B[c].x * v.x;
+                            }
+                        } else if constexpr (CPLX) {
+                            accr[c] = fmaf(Aw[k].x, v.x, fmaf(-Aw[k].y, v.y, accr[c]));
+                            acci[c] = fmaf(Aw[k].x, v.y, fmaf(Aw[k].y, v.x, acci[c]));
+                        } else {
+                            accr[c] = fmaf(Aw[k].x, v.x, accr[c]);
+                        }
+                    }
+                }
+                if (MODE == USTB_DIM_NONE && live && A.cube) {
+                    // units skipped by a zero apodization are zero, as in das_c
+#pragma unroll
+                    for (int c = 0; c < CG; ++c)
+#pragma unroll
+                        for (int k = 0; k < KW; ++k)
+                            if (c < cg && k < kw && !(s_act_n[c] && s_act_w[k])) {
+                                const int64_t o = p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f;
+                                if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = make_float2(0.f, 0.f);
+                                else reinterpret_cast<float*>(A.cube)[o] = 0.f;
+                            }
+                }
+            }
+            if (MODE == USTB_DIM_TRANSMIT) {
+#pragma unroll
+                for (int c = 0; c < CG; ++c) {
+                    if (c >= cg) continue;
+                    float2 y;
+                    if constexpr (CPLX) y = cmul(cmul(B[c], make_float2(accr[c], acci[c])), ph);
+                    else y = make_float2(B[c].x * accr[c], 0.f);
+                    if (live && A.cube) {
+                        const int64_t o = p + A.rx_f * (n0 + c) + A.f_f * f;
+                        if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = y;
+                        else reinterpret_cast<float*>(A.cube)[o] = y.x;
+                    }
+                    if constexpr (EPI) {
+                        eS.x += y.x;
+                        eS.y += y.y;
+                        eI += y.x * y.x + y.y * y.y;
+                        eM += rxapo[c] > A.cf_thr ? 1.f : 0.f;
+                        const float re = y.x;
+                        eR += msign(re) * sqrtf(fabsf(re));
+                        eQ += fabsf(re);
+                    }
+                }
+            }
+        }
+        if constexpr (EPI) {
+            if (live) {
+                const int64_t o = p + P * f;
+                float cf = (eS.x * eS.x + eS.y * eS.y) / eI * (1.f / eM);
+                if (cf != cf) cf = 0.f;  // NaN -> 0 (coherence_factor.m:132)
+                if (A.o_das) A.o_das[o] = eS;
+                if (A.o_cf) A.o_cf[o] = cf;
+                if (A.o_cfimg) A.o_cfimg[o] = make_float2(cf * eS.x, cf * eS.y);
+                if (A.o_sdmas) A.o_sdmas[o] = 0.5f * (eR * eR - eQ);
+            }
+        }
+    }
+}
+
+template <int MODE, bool CPLX, int ST, bool EPI>
+int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
+    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
+    constexpr int NS = (ORDER_A ? 2 * 16 : 8 * 4);
+    const size_t smem = (size_t)NS * kSlot * (CPLX ? 16 : 8);
+    auto kern = das_fast_kernel<MODE, CPLX, ST, EPI>;
+    USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)n_tiles, (unsigned)F);
+    kern<<<grid, kTile, smem, s>>>(A);
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
+template <bool CPLX, int ST>
+int dispatch_mode(int dim, int epi, const Params& A, int64_t nt, int64_t F, cudaStream_t s) {
+    switch (dim) {
+        case USTB_DIM_NONE: return launch<USTB_DIM_NONE, CPLX, ST, false>(A, nt, F, s);
+        case USTB_DIM_RECEIVE: return launch<USTB_DIM_RECEIVE, CPLX, ST, false>(A, nt, F, s);
+        case USTB_DIM_TRANSMIT:
+            if constexpr (CPLX)
+                if (epi) return launch<USTB_DIM_TRANSMIT, CPLX, ST, true>(A, nt, F, s);
+            return launch<USTB_DIM_TRANSMIT, CPLX, ST, false>(A, nt, F, s);
+        default: return launch<USTB_DIM_BOTH, CPLX, ST, false>(A, nt, F, s);
+    }
+}
+
+}  // namespace
+
+extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
+                             int64_t W, int64_t F, const ustb_das_geometry* g, int32_t dimension,
+                             int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(g && out, USTB_E_ARG, "geometry and outputs must be given");
+    USTB_REQUIRE(dimension >= 0 && dimension <= 3, USTB_E_ARG, "Unknown sum mode %d", (int)dimension);
+    USTB_REQUIRE(storage >= 0 && storage <= 2, USTB_E_DTYPE, "unknown storage type %d", (int)storage);
+    USTB_REQUIRE(is_complex == 0 || is_complex == 1, USTB_E_ARG, "is_complex must be 0 or 1");
+    USTB_REQUIRE(L >= 0 && N >= 0 && W >= 0 && F >= 0, USTB_E_SHAPE, "negative size");
+    USTB_REQUIRE(g->n_elements == N && g->n_waves == W, USTB_E_SHAPE,
+                 "geometry has %lld elements / %lld waves, channel data %lld / %lld",
+                 (long long)g->n_elements, (long long)g->n_waves, (long long)N, (long long)W);
+    USTB_REQUIRE(is_complex || !(fabsf(g->fd) > 1e-6f), USTB_E_DTYPE,
+                 "The modulation frequency > 0 but the input data is real. Check inputs.");
+    USTB_REQUIRE(!epilogue || (dimension == USTB_DIM_TRANSMIT && is_complex), USTB_E_ARG,
+                 "the coherence-factor / DMAS epilogue needs dimension.transmit and complex data");
+    USTB_REQUIRE(flags, USTB_E_ARG, "flags pointer is NULL");
+    USTB_REQUIRE(F <= 65535, USTB_E_SHAPE, "at most 65535 frames per call");
+    USTB_REQUIRE(g->n_tiles <= INT32_MAX, USTB_E_SHAPE, "too many tiles");
+    USTB_REQUIRE(g->sound_speed > 0.f && g->fs > 0.f, USTB_E_ARG, "sound speed and fs must be > 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    USTB_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t), s));
+    if (g->n_tiles == 0 || F == 0 || g->n_pixels == 0) return USTB_OK;
+    USTB_REQUIRE(g->element_xyz && g->pixel_xyz && g->tile_pixels && (W == 0 || g->waves), USTB_E_ARG,
+                 "a geometry pointer is NULL");
+    USTB_REQUIRE(L == 0 || N == 0 || W == 0 || ch, USTB_E_ARG, "channel data pointer is NULL");
+    const int64_t P = g->n_pixels;
+    if (L == 0 || N == 0 || W == 0) {
+        const int64_t nout = out_elems(dimension, P, N, W, F);
+        if (out->cube && nout)
+            USTB_CUDA(cudaMemsetAsync(out->cube, 0, (size_t)nout * (is_complex ? 8 : 4), s));
+        return USTB_OK;
+    }
+    Params A;
+    A.ch = ch;
+    A.L = L; A.N = N; A.W = W; A.F = F; A.P = P;
+    A.el = g->element_xyz;
+    A.px = g->pixel_xyz;
+    A.tiles = g->tile_pixels;
+    A.waves = g->waves;
+    A.tx_delay_tab = g->tx_delay_table;
+    A.tx_apo_tab = g->tx_apo_table;
+    A.rx_apo_tab = g->rx_apo_table;
+    A.pix_phase = reinterpret_cast<const float2*>(g->pixel_phase);
+    A.fs = g->fs; A.t0 = g->t0; A.fd = (fabsf(g->fd) > 1e-6f) ? g->fd : 0.f;
+    A.inv_c = 1.f / g->sound_speed;
+    A.lens = g->lens_delay;
+    A.rx_window = g->rx_window;
+    A.fnx = g->rx_f_number[0]; A.fny = g->rx_f_number[1];
+    A.minx = g->rx_min_aperture[0]; A.miny = g->rx_min_aperture[1];
+    A.maxx = g->rx_max_aperture[0]; A.maxy = g->rx_max_aperture[1];
+    A.rx_origin = g->rx_use_origin;
+    A.ox = g->rx_origin[0]; A.oy = g->rx_origin[1]; A.oz = g->rx_origin[2];
+    A.cf_thr = g->cf_threshold;
+    A.cube = out->cube;
+    A.o_das = reinterpret_cast<float2*>(out->das);
+    A.o_cf = out->cf;
+    A.o_cfimg = reinterpret_cast<float2*>(out->cf_image);
+    A.o_sdmas = out->sdmas;
+    const OutStrides os = out_strides(dimension, P, N, W);
+    A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
+    A.flags = flags;
+    const int64_t nt = g->n_tiles;
+    if (is_complex) {
+        switch (storage) {
+            case USTB_STORE_F32: return dispatch_mode<true, USTB_STORE_F32>(dimension, epilogue, A, nt, F, s);
+            case USTB_STORE_F16: return dispatch_mode<true, USTB_STORE_F16>(dimension, epilogue, A, nt, F, s);
+            default: return dispatch_mode<true, USTB_STORE_BF16>(dimension, epilogue, A, nt, F, s);
+        }
+    }
+    switch (storage) {
+        case USTB_STORE_F32: return dispatch_mode<false, USTB_STORE_F32>(dimension, 0, A, nt, F, s);
+        case USTB_STORE_F16: return dispatch_mode<false, USTB_STORE_F16>(dimension, 0, A, nt, F, s);
+        default: return dispatch_mode<false, USTB_STORE_BF16>(dimension, 0, A, nt, F, s);
+    }
+}

@@ -85,7 +85,12 @@ class DAS:
         self.beamformed_data = None
         # GB300 additions
         self.precision = Precision.fp32
+        # "table": the das_c drop-in on single-precision tables (bit-level das_c semantics);
+        # "fast": on-the-fly geometry, channel data stored as `precision`
+        self.engine = "table"
         self.rf_mode = "analytic"  # "analytic" (das.m semantics) | "real" (real RF in, real out)
+        self.epilogue = False      # fast engine, dimension.transmit: also CF / simplified-DMAS
+        self.epilogue_outputs = None
 
     # -- tables ---------------------------------------------------------------
     def tables(self):
@@ -113,6 +118,8 @@ class DAS:
     def go(self) -> BeamformedData:
         if Code(int(self.code)) != Code.gb300:
             raise ValueError("this beamformer implements code.gb300 only")
+        if self.engine == "fast" or Precision(int(self.precision)) != Precision.fp32:
+            return self._go_fast()
         cd, scan = self.channel_data, self.scan
         dev = torch.device("cuda", int(self.gpu_id))
         fs = float(np.float32(cd.sampling_frequency))
@@ -120,14 +127,7 @@ class DAS:
         fd = float(np.float32(cd.modulation_frequency))
         w0 = 2 * math.pi * fd
         tx_apo, rx_apo, tx_delay, rx_delay = self.tables()
-        ch = channel_tensor(cd.data, dev)
-        if abs(w0) < np.finfo(np.float64).eps:
-            if ch.is_complex():
-                pass
-            elif self.rf_mode == "analytic":
-                ch = hilbert_last(ch)
-        elif not ch.is_complex():
-            raise ValueError("The modulation frequency > 0 but the input data is real. Check inputs.")
+        ch = self._channels(dev, w0)
         T = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
         t_start = time.perf_counter()
         out = kernels.das_table_f32(ch, fs, t0, T(tx_apo), T(rx_apo), T(tx_delay), T(rx_delay),
@@ -138,4 +138,45 @@ class DAS:
         torch.cuda.synchronize(dev)
         self.elapsed_time = time.perf_counter() - t_start
         self.beamformed_data = BeamformedData(scan, kernels.to_matlab_order(out))
+        return self.beamformed_data
+
+    def _channels(self, dev, w0):
+        ch = channel_tensor(self.channel_data.data, dev)
+        if abs(w0) < np.finfo(np.float64).eps:
+            if not ch.is_complex() and self.rf_mode == "analytic":
+                ch = hilbert_last(ch)
+        elif not ch.is_complex():
+            raise ValueError("The modulation frequency > 0 but the input data is real. Check inputs.")
+        return ch
+
+    def fast_geometry(self, dev) -> "fast.FastGeometry":
+        from . import fast
+
+        cd = self.channel_data
+        fd = float(np.float32(cd.modulation_frequency))
+        ph = self.pixel_phase() if abs(fd) > 0 else None
+        return fast.FastGeometry(cd.probe, self.scan, cd.sequence, float(cd.sampling_frequency),
+                                 float(cd.initial_time), fd, float(cd.sound_speed), dev,
+                                 self.receive_apodization, self.transmit_apodization,
+                                 self.lens_delay, self.spherical_transmit_delay_model,
+                                 self.pw_margin, self.blending_power, pixel_phase=ph)
+
+    def _go_fast(self) -> BeamformedData:
+        from . import fast
+
+        cd, scan = self.channel_data, self.scan
+        dev = torch.device("cuda", int(self.gpu_id))
+        fd = float(np.float32(cd.modulation_frequency))
+        ch = self._channels(dev, 2 * math.pi * fd)
+        geom = self.fast_geometry(dev)
+        prec = Precision(int(self.precision))
+        t_start = time.perf_counter()
+        st = fast.convert_channels(ch, prec)
+        F, W, N, L = ch.shape
+        epi = bool(self.epilogue) and int(self.dimension) == int(Dimension.transmit)
+        outs = fast.das_fast(st, prec, ch.is_complex(), geom, self.dimension, F=F, epilogue=epi, L=L)
+        torch.cuda.synchronize(dev)
+        self.elapsed_time = time.perf_counter() - t_start
+        self.epilogue_outputs = {k: v for k, v in outs.items() if k not in ("cube", "flags")} if epi else None
+        self.beamformed_data = BeamformedData(scan, kernels.to_matlab_order(outs["cube"]))
         return self.beamformed_data

@@ -1,0 +1,358 @@
+"""Fast path: reduced-precision channel storage and on-the-fly geometry.
+
+``FastGeometry`` turns a probe / scan / sequence / apodization description
+(the inputs of midprocess.das) into the device-side ``ustb_das_geometry`` of
+the C-ABI: element and pixel positions, one ``ustb_wave`` per transmit event,
+and a tile map that groups pixels into compact tiles of 256 so that every
+(channel, wave) sample window of a tile stays short (``plan_tiles``).  Anything
+the kernel cannot form on the fly (focused waves in the hybrid margin, the
+unified and blended models, tilted or vector apodizations) is passed as a
+single-precision table computed by ``geometry`` exactly as das.m does.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib, geometry
+from .enums import Dimension, Precision, SphericalTransmitDelayModel as STDM, Wavefront, Window
+from .geometry import Apodization
+from .uff import LinearScan, Probe, Scan, SectorScan, Wave
+
+TILE = 256
+SLOT_HALF = 63          # kernel: max relative delay (samples) of each component
+SPAN_LIMIT = 58.0       # planner: keep tile spans below this many samples
+STORE = {Precision.fp32: 0, Precision.fp16: 1, Precision.bf16: 2}
+TORCH_STORE = {Precision.fp32: torch.float32, Precision.fp16: torch.float16, Precision.bf16: torch.bfloat16}
+FLAG_WINDOW_OVERFLOW = 1
+
+
+class CWave(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("dir", ctypes.c_float * 3), ("src", ctypes.c_float * 3),
+                ("offset", ctypes.c_float), ("sound_speed", ctypes.c_float), ("delay", ctypes.c_float),
+                ("apodization", ctypes.c_float), ("reserved", ctypes.c_float)]
+
+
+class CGeometry(ctypes.Structure):
+    _fields_ = [("n_elements", ctypes.c_int64), ("element_xyz", ctypes.c_void_p),
+                ("n_pixels", ctypes.c_int64), ("pixel_xyz", ctypes.c_void_p),
+                ("n_tiles", ctypes.c_int64), ("tile_pixels", ctypes.c_void_p),
+                ("n_waves", ctypes.c_int64), ("waves", ctypes.c_void_p),
+                ("tx_delay_table", ctypes.c_void_p), ("tx_apo_table", ctypes.c_void_p),
+                ("rx_apo_table", ctypes.c_void_p), ("pixel_phase", ctypes.c_void_p),
+                ("fs", ctypes.c_float), ("t0", ctypes.c_float), ("fd", ctypes.c_float),
+                ("sound_speed", ctypes.c_float), ("lens_delay", ctypes.c_float),
+                ("rx_window", ctypes.c_int32), ("rx_f_number", ctypes.c_float * 2),
+                ("rx_min_aperture", ctypes.c_float * 2), ("rx_max_aperture", ctypes.c_float * 2),
+                ("rx_use_origin", ctypes.c_int32), ("rx_origin", ctypes.c_float * 3),
+                ("cf_threshold", ctypes.c_float)]
+
+
+class COutputs(ctypes.Structure):
+    _fields_ = [("cube", ctypes.c_void_p), ("das", ctypes.c_void_p), ("cf", ctypes.c_void_p),
+                ("cf_image", ctypes.c_void_p), ("sdmas", ctypes.c_void_p)]
+
+
+assert ctypes.sizeof(CWave) == 48
+
+
+# ---------------------------------------------------------------------------
+# tile planning
+# ---------------------------------------------------------------------------
+
+def _diag(xyz: np.ndarray) -> float:
+    return float(np.linalg.norm(xyz.max(axis=0) - xyz.min(axis=0)))
+
+
+def _split_blocks(grid_idx: np.ndarray, xyz: np.ndarray, limit: float, out: list):
+    """Recursively split an index block (ndarray of pixel ids, any dims) until its
+    bounding-box diagonal is below ``limit`` metres (or it is one pixel)."""
+    stack = [grid_idx]
+    while stack:
+        b = stack.pop()
+        flat = b.ravel()
+        if flat.size == 0:
+            continue
+        if flat.size == 1 or _diag(xyz[flat]) <= limit:
+            out.append(flat)
+            continue
+        # split the axis with the largest physical extent
+        ext = []
+        for ax in range(b.ndim):
+            if b.shape[ax] < 2:
+                ext.append(-1.0)
+                continue
+            first = np.take(b, 0, axis=ax).ravel()
+            last = np.take(b, b.shape[ax] - 1, axis=ax).ravel()
+            ext.append(float(np.linalg.norm(xyz[last].mean(0) - xyz[first].mean(0))))
+        ax = int(np.argmax(ext))
+        h = b.shape[ax] // 2
+        stack.append(np.take(b, range(0, h), axis=ax))
+        stack.append(np.take(b, range(h, b.shape[ax]), axis=ax))
+
+
+def _block_dims(spacing, shape, ndim_target=TILE):
+    """Block shape with product <= 256 balancing the physical extents."""
+    sp = [max(s, 1e-12) for s in spacing]
+    dims = [1] * len(sp)
+    while True:
+        best, bi = None, None
+        for i in range(len(sp)):
+            prod = int(np.prod(dims)) * 2
+            if prod > ndim_target or dims[i] >= shape[i]:
+                continue
+            ext = dims[i] * sp[i]
+            if best is None or ext < best:
+                best, bi = ext, i
+        if bi is None:
+            return dims
+        dims[bi] *= 2
+
+
+def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SPAN_LIMIT) -> np.ndarray:
+    """Group pixel indices into tiles of 256 lanes (-1 = idle lane).
+
+    A tile's receive and transmit delay spans are bounded by its bounding-box
+    diagonal; tiles are shrunk until that diagonal is below
+    ``span_limit`` samples of one-way travel."""
+    xyz = scan.xyz
+    P = scan.N_pixels
+    limit = span_limit * sound_speed / fs
+    if isinstance(scan, LinearScan):
+        shape = (scan.z_axis.size, scan.x_axis.size, scan.y_axis.size)
+        spacing = [np.mean(np.abs(np.diff(a))) if a.size > 1 else 0.0
+                   for a in (scan.z_axis, scan.x_axis, scan.y_axis)]
+    elif isinstance(scan, SectorScan):
+        shape = (scan.depth_axis.size, scan.azimuth_axis.size, scan.elevation_axis.size)
+        dr = np.mean(np.abs(np.diff(scan.depth_axis))) if scan.depth_axis.size > 1 else 0.0
+        rmax = float(np.max(np.abs(scan.depth_axis)))
+        da = rmax * (np.mean(np.abs(np.diff(scan.azimuth_axis))) if scan.azimuth_axis.size > 1 else 0.0)
+        de = rmax * (np.mean(np.abs(np.diff(scan.elevation_axis))) if scan.elevation_axis.size > 1 else 0.0)
+        spacing = [dr, da, de]
+    else:
+        # unstructured: order by a coarse spatial grid, then chunk
+        cell = limit / 2
+        key = np.floor((xyz - xyz.min(0)) / cell).astype(np.int64)
+        order = np.lexsort((key[:, 2], key[:, 0], key[:, 1]))
+        blocks = []
+        for i in range(0, P, TILE):
+            _split_blocks(order[i:i + TILE], xyz, limit, blocks)
+        return _pack(blocks)
+    idx = np.arange(P).reshape(shape, order="F")
+    bd = _block_dims(spacing, shape)
+    blocks = []
+    for i in range(0, shape[0], bd[0]):
+        for j in range(0, shape[1], bd[1]):
+            for k in range(0, shape[2], bd[2]):
+                _split_blocks(idx[i:i + bd[0], j:j + bd[1], k:k + bd[2]], xyz, limit, blocks)
+    return _pack(blocks)
+
+
+def _pack(blocks) -> np.ndarray:
+    T = len(blocks)
+    tiles = np.full((T, TILE), -1, dtype=np.int32)
+    for t, b in enumerate(blocks):
+        tiles[t, :b.size] = b
+    return tiles
+
+
+# ---------------------------------------------------------------------------
+# geometry
+# ---------------------------------------------------------------------------
+
+def _wave_struct(wave: Wave, kind: int, apo: float, offset: float = 0.0) -> CWave:
+    s = wave.source
+    cw = CWave()
+    cw.kind = kind
+    if kind == 0:
+        ce = math.cos(s.elevation)
+        cw.dir[0] = math.sin(s.azimuth) * ce
+        cw.dir[1] = math.sin(s.elevation)
+        cw.dir[2] = math.cos(s.azimuth) * ce
+    elif kind == 1:
+        cw.src[0], cw.src[1], cw.src[2] = s.x, s.y, s.z
+    cw.offset = offset
+    cw.sound_speed = wave.sound_speed
+    cw.delay = wave.delay
+    cw.apodization = apo
+    return cw
+
+
+class FastGeometry:
+    """Device-side geometry of one request for ``ustb_das_fast``."""
+
+    def __init__(self, probe: Probe, scan: Scan, sequence: Sequence[Wave], fs: float, t0: float,
+                 fd: float, sound_speed: float, device, rx_apodization: Optional[Apodization] = None,
+                 tx_apodization: Optional[Apodization] = None, lens_delay: float = 0.0,
+                 model: STDM = STDM.hybrid, pw_margin: float = 1e-3, blending_power: float = 0.5,
+                 pixel_phase: Optional[np.ndarray] = None, cf_threshold: float = 0.16,
+                 tiles: Optional[np.ndarray] = None):
+        dev = torch.device(device)
+        rx = rx_apodization or Apodization()
+        tx = tx_apodization or Apodization()
+        self.probe, self.scan, self.sequence = probe, scan, list(sequence)
+        P, N, W = scan.N_pixels, probe.N_elements, len(self.sequence)
+        self.P, self.N, self.W = P, N, W
+        f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+        self.d_el = f32(probe.xyz)
+        self.d_px = f32(scan.xyz)
+        self.tiles = plan_tiles(scan, fs, sound_speed) if tiles is None else tiles
+        self.d_tiles = torch.from_numpy(self.tiles).to(dev)
+
+        # transmit events
+        table_waves = []
+        structs = []
+        tx_const = self._tx_apodization_constants(tx)
+        for w, wave in enumerate(self.sequence):
+            wf = Wavefront(int(wave.wavefront))
+            s = wave.source
+            a = 1.0 if tx_const is None else float(tx_const[w])
+            if wf == Wavefront.plane or (wf == Wavefront.spherical and math.isinf(s.distance)):
+                structs.append(_wave_struct(wave, 0, a))
+            elif wf == Wavefront.photoacoustic:
+                structs.append(_wave_struct(wave, 2, a))
+            elif s.z < 0:
+                structs.append(_wave_struct(wave, 1, a, -abs(s.distance)))
+            else:
+                m = STDM(int(model))
+                band = np.any((scan.z < s.z + pw_margin) & (scan.z > s.z - pw_margin))
+                if m == STDM.spherical or (m == STDM.hybrid and not band):
+                    structs.append(_wave_struct(wave, 1, a, s.distance))
+                else:
+                    structs.append(_wave_struct(wave, 3, a))
+                    table_waves.append(w)
+        arr = (CWave * max(W, 1))(*structs)
+        self.d_waves = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+        self.d_txdelay = None
+        if table_waves:
+            td = geometry.transmit_delay(self.sequence, scan, model, pw_margin, blending_power,
+                                         tx.f_number).astype(np.float32)
+            self.d_txdelay = f32(td.T)
+        self.d_txapo = None
+        if tx_const is None:
+            self.d_txapo = f32(tx.wave_apodization(self.sequence, scan).T)
+
+        # receive apodization
+        self.d_rxapo = None
+        self.rx_window = int(rx.window)
+        on_the_fly = (rx.apodization_vector is None and rx.window not in (Window.sta, Window.scanline)
+                      and rx.tilt == (0.0, 0.0))
+        if not on_the_fly:
+            self.d_rxapo = f32(rx.aperture_apodization(probe, scan).T)
+            self.rx_window = 0
+        origin = rx.origin
+        if origin is None and isinstance(scan, SectorScan):
+            origin = scan.origin
+        self.d_phase = None
+        if pixel_phase is not None:
+            self.d_phase = torch.from_numpy(np.asarray(pixel_phase, np.complex64)).to(dev)
+
+        g = CGeometry()
+        g.n_elements, g.element_xyz = N, self.d_el.data_ptr()
+        g.n_pixels, g.pixel_xyz = P, self.d_px.data_ptr()
+        g.n_tiles, g.tile_pixels = self.tiles.shape[0], self.d_tiles.data_ptr()
+        g.n_waves, g.waves = W, self.d_waves.data_ptr()
+        g.tx_delay_table = self.d_txdelay.data_ptr() if self.d_txdelay is not None else None
+        g.tx_apo_table = self.d_txapo.data_ptr() if self.d_txapo is not None else None
+        g.rx_apo_table = self.d_rxapo.data_ptr() if self.d_rxapo is not None else None
+        g.pixel_phase = self.d_phase.data_ptr() if self.d_phase is not None else None
+        g.fs, g.t0, g.fd = fs, t0, fd
+        g.sound_speed, g.lens_delay = sound_speed, lens_delay
+        g.rx_window = self.rx_window
+        g.rx_f_number[0], g.rx_f_number[1] = rx.f_number
+        g.rx_min_aperture[0], g.rx_min_aperture[1] = rx.minimum_aperture
+        g.rx_max_aperture[0], g.rx_max_aperture[1] = rx.maximum_aperture
+        g.rx_use_origin = 1 if origin is not None else 0
+        if origin is not None:
+            g.rx_origin[0], g.rx_origin[1], g.rx_origin[2] = origin.x, origin.y, origin.z
+        g.cf_threshold = cf_threshold
+        self.c = g
+        self.device = dev
+
+    def _tx_apodization_constants(self, tx: Apodization):
+        """Per-wave constant tx apodization when it does not vary over pixels, else None."""
+        W = len(self.sequence)
+        if tx.apodization_vector is not None:
+            v = np.asarray(tx.apodization_vector, np.float64).ravel()
+            return v if v.size == W else None
+        if tx.window == Window.none:
+            return np.ones(W)
+        if tx.window == Window.scanline:
+            return None
+        planes = all(Wavefront(int(w.wavefront)) == Wavefront.plane or math.isinf(w.source.distance)
+                     for w in self.sequence)
+        if not planes:
+            return None
+        one = Scan([0.0], [0.0], [1.0])
+        return tx.wave_apodization(self.sequence, one)[0]
+
+    def units(self, F: int = 1) -> int:
+        return self.P * self.N * self.W * F
+
+
+def convert_channels(src: torch.Tensor, precision: Precision, scale: float = 1.0) -> torch.Tensor:
+    """Channel data -> device storage type through ``ustb_convert_channels``.
+
+    ``src``: complex64 / float32 / int16 / float16 CUDA tensor in the ABI layout (for
+    int16 I/Q the last dimension holds interleaved I, Q).  Complex input keeps its
+    shape and becomes (..., 2) real pairs of the storage type."""
+    if src.is_complex():
+        flat = torch.view_as_real(src)
+        st = 0
+    elif src.dtype == torch.float32:
+        flat, st = src, 0
+    elif src.dtype == torch.int16:
+        flat, st = src, 1
+    elif src.dtype == torch.float16:
+        flat, st = src, 2
+    else:
+        raise TypeError(f"unsupported source dtype {src.dtype}")
+    dst = torch.empty(flat.shape, dtype=TORCH_STORE[Precision(precision)], device=src.device)
+    with torch.cuda.device(src.device):
+        _lib.call("ustb_convert_channels", flat.data_ptr(), st, dst.data_ptr(), STORE[Precision(precision)],
+                  flat.numel(), float(scale), torch.cuda.current_stream(src.device).cuda_stream)
+    return dst
+
+
+def das_fast(ch: torch.Tensor, precision: Precision, is_complex: bool, geom: FastGeometry,
+             dimension=Dimension.both, F: int = 1, epilogue: bool = False, cube: bool = True,
+             flags: Optional[torch.Tensor] = None, check: bool = True, L: Optional[int] = None):
+    """Run ``ustb_das_fast``.  ``ch`` holds [L,N,W,F] samples of the storage type
+    (complex: trailing (re, im) pairs).  Returns a dict of output tensors in the ABI
+    layout: 'cube' (F, Wk, Nk, P) and, with the epilogue, 'das', 'cf', 'cf_image',
+    'sdmas' of shape (F, P)."""
+    dev = ch.device
+    P, N, W = geom.P, geom.N, geom.W
+    if L is None:
+        L = ch.numel() // ((2 if is_complex else 1) * N * W * F)
+    outs = {}
+    o = COutputs()
+    dt = torch.complex64 if is_complex else torch.float32
+    if cube:
+        from .kernels import out_shape_abi
+
+        outs["cube"] = torch.empty(out_shape_abi(P, N, W, F, dimension), dtype=dt, device=dev)
+        o.cube = outs["cube"].data_ptr()
+    if epilogue:
+        outs["das"] = torch.empty((F, P), dtype=torch.complex64, device=dev)
+        outs["cf"] = torch.empty((F, P), dtype=torch.float32, device=dev)
+        outs["cf_image"] = torch.empty((F, P), dtype=torch.complex64, device=dev)
+        outs["sdmas"] = torch.empty((F, P), dtype=torch.float32, device=dev)
+        o.das, o.cf = outs["das"].data_ptr(), outs["cf"].data_ptr()
+        o.cf_image, o.sdmas = outs["cf_image"].data_ptr(), outs["sdmas"].data_ptr()
+    if flags is None:
+        flags = torch.zeros(1, dtype=torch.int32, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call("ustb_das_fast", ch.data_ptr(), STORE[Precision(precision)], int(is_complex), L, N, W, F,
+                  ctypes.byref(geom.c), int(dimension), int(epilogue), ctypes.byref(o), flags.data_ptr(),
+                  torch.cuda.current_stream(dev).cuda_stream)
+    if check:
+        fl = int(flags.item())
+        if fl & FLAG_WINDOW_OVERFLOW:
+            raise _lib.UstbError(7, "a tile's sample window overflowed its slot; plan smaller tiles")
+    outs["flags"] = flags
+    return outs
