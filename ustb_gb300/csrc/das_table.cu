@@ -9,9 +9,9 @@
 // b = s - floor(s), phase = fl(wd * delay).  Only the order of the final sums
 // and FMA contraction in the interpolation/rotation differ (a few ulp).
 //
-// Loop order: channels outer, waves inner (rx delay/apodization read once per
-// pixel-channel from HBM, the pixel's tx row re-read from L1), except for
-// dimension.receive, which keeps waves and sums channels (waves outer).
+// Loop order: for dimension.both/.receive, chunks of WC waves outer (their tx
+// values in registers) and channels inner (rx values re-read once per chunk);
+// for .transmit/.none, channels outer and wave chunks inner.
 #include "common.cuh"
 #include "phasor.cuh"
 
@@ -42,49 +42,6 @@ struct Acc {
     }
 };
 
-// Evaluate one (pixel, channel, wave) unit for frames [f0, f0+nf) and add it
-// into `acc` (which the caller zeroed for dimension.none).
-template <bool CPLX, int FC>
-__device__ __forceinline__ void unit(const TableArgs& A, int64_t n, int64_t w, int64_t f0, int nf,
-                                     float txd, float txa, float rxd, float rxa,
-                                     Acc<CPLX, FC>& acc) {
-    const float delay = __fadd_rn(txd, rxd);
-    const float apo = __fmul_rn(txa, rxa);
-    const float denay = __fmul_rn(__fsub_rn(delay, A.t0), A.fs);
-    const int n0 = __float2int_rz(denay);
-    if (!(n0 > 0 && (int64_t)n0 < A.L - 1)) return;
-    const float b = __fsub_rn(denay, floorf(denay));
-    const float a = __fsub_rn(1.0f, b);
-    const int64_t base = A.L * n + A.LN * w + n0 + f0 * A.LNW;
-    if (CPLX) {
-        float c, s;
-        ustb::expi_reduced(__fmul_rn(A.wd, delay), c, s);
-        const float wr = c * apo, wi = s * apo;
-        const float2* x = reinterpret_cast<const float2*>(A.ch) + base;
-#pragma unroll
-        for (int f = 0; f < FC; ++f) {
-            if (f < nf) {
-                const float2 x0 = __ldg(x + f * A.LNW);
-                const float2 x1 = __ldg(x + f * A.LNW + 1);
-                const float vr = fmaf(b, x1.x, a * x0.x);
-                const float vi = fmaf(b, x1.y, a * x0.y);
-                acc.re[f] = fmaf(wr, vr, fmaf(-wi, vi, acc.re[f]));
-                acc.im[f] = fmaf(wr, vi, fmaf(wi, vr, acc.im[f]));
-            }
-        }
-    } else {
-        const float* x = reinterpret_cast<const float*>(A.ch) + base;
-#pragma unroll
-        for (int f = 0; f < FC; ++f) {
-            if (f < nf) {
-                const float x0 = __ldg(x + f * A.LNW);
-                const float x1 = __ldg(x + f * A.LNW + 1);
-                acc.re[f] = fmaf(apo, fmaf(b, x1, a * x0), acc.re[f]);
-            }
-        }
-    }
-}
-
 template <bool CPLX, int FC>
 __device__ __forceinline__ void store(const TableArgs& A, int64_t idx, int64_t f0, int nf,
                                       const Acc<CPLX, FC>& acc) {
@@ -100,49 +57,124 @@ __device__ __forceinline__ void store(const TableArgs& A, int64_t idx, int64_t f
     }
 }
 
+// Waves are processed in chunks of WC whose tx delay/apodization sit in
+// registers; for each channel the WC units of the chunk are independent.  They
+// are evaluated branch-free: every unit loads from a safe sample index and an
+// invalid or zero-apodization unit's contribution is selected away (not
+// multiplied by zero, so non-finite samples behave as in das_c, which skips
+// those units).  All WC sample loads are then in flight together.
+constexpr int WC = 8;
+
+template <bool CPLX, int FC, bool PER_WAVE, int NACC>
+__device__ __forceinline__ void chunk_units(const TableArgs& A, int64_t n, int64_t w0, int wc, int64_t f0,
+                                            int nf, const float* txd, const float* txa, float rxd, float rxa,
+                                            Acc<CPLX, FC>* acc) {
+    float a[WC], b[WC], wr[WC], wi[WC];
+    int64_t base[WC];
+    bool ok[WC];
+#pragma unroll
+    for (int k = 0; k < WC; ++k) {
+        const float delay = __fadd_rn(txd[k], rxd);
+        const float apo = __fmul_rn(txa[k], rxa);
+        const float denay = __fmul_rn(__fsub_rn(delay, A.t0), A.fs);
+        const int n0 = __float2int_rz(denay);
+        ok[k] = k < wc && txa[k] != 0.0f && rxa != 0.0f && n0 > 0 && (int64_t)n0 < A.L - 1;
+        b[k] = __fsub_rn(denay, floorf(denay));
+        a[k] = __fsub_rn(1.0f, b[k]);
+        base[k] = A.L * n + A.LN * (w0 + (k < wc ? k : 0)) + (ok[k] ? n0 : 1) + f0 * A.LNW;
+        if (CPLX) {
+            float c, s;
+            ustb::expi_reduced(__fmul_rn(A.wd, delay), c, s);
+            wr[k] = c * apo;
+            wi[k] = s * apo;
+        } else {
+            wr[k] = apo;
+            wi[k] = 0.f;
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < FC; ++f) {
+        if (f >= nf) continue;
+#pragma unroll
+        for (int k = 0; k < WC; ++k) {
+            Acc<CPLX, FC>& ac = acc[PER_WAVE ? k : 0];
+            if (CPLX) {
+                const float2* x = reinterpret_cast<const float2*>(A.ch) + base[k] + f * A.LNW;
+                const float2 x0 = __ldg(x), x1 = __ldg(x + 1);
+                const float vr = fmaf(b[k], x1.x, a[k] * x0.x);
+                const float vi = fmaf(b[k], x1.y, a[k] * x0.y);
+                const float nr = fmaf(wr[k], vr, fmaf(-wi[k], vi, ac.re[f]));
+                const float ni = fmaf(wr[k], vi, fmaf(wi[k], vr, ac.im[f]));
+                ac.re[f] = ok[k] ? nr : ac.re[f];
+                ac.im[f] = ok[k] ? ni : ac.im[f];
+            } else {
+                const float* x = reinterpret_cast<const float*>(A.ch) + base[k] + f * A.LNW;
+                const float x0 = __ldg(x), x1 = __ldg(x + 1);
+                const float nr = fmaf(wr[k], fmaf(b[k], x1, a[k] * x0), ac.re[f]);
+                ac.re[f] = ok[k] ? nr : ac.re[f];
+            }
+        }
+    }
+}
+
 template <int MODE, bool CPLX, int FC>
 __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) {
     const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     if (p >= A.P) return;
     const int64_t P = A.P;
-    Acc<CPLX, FC> acc;
+    constexpr bool PER_WAVE = (MODE == USTB_DIM_RECEIVE || MODE == USTB_DIM_NONE);
+    constexpr int NACC = PER_WAVE ? WC : 1;
+    Acc<CPLX, FC> acc[NACC];
+    float txd[WC], txa[WC];
+    auto load_tx = [&](int64_t w0, int wc) {
+#pragma unroll
+        for (int k = 0; k < WC; ++k) {
+            txa[k] = k < wc ? __ldg(A.apo_tx + P * (w0 + k) + p) : 0.f;
+            txd[k] = k < wc ? __ldg(A.d_tx + P * (w0 + k) + p) : 0.f;
+        }
+    };
     for (int64_t f0 = 0; f0 < A.F; f0 += FC) {
         const int nf = (int)min((int64_t)FC, A.F - f0);
-        if (MODE == USTB_DIM_RECEIVE) {
-            for (int64_t w = 0; w < A.W; ++w) {
-                const float txd = __ldg(A.d_tx + P * w + p);
-                const float txa = __ldg(A.apo_tx + P * w + p);
-                acc.zero();
-                if (txa != 0.0f) {
-                    for (int64_t n = 0; n < A.N; ++n) {
-                        const float rxa = __ldg(A.apo_rx + P * n + p);
-                        if (rxa == 0.0f) continue;
-                        const float rxd = __ldg(A.d_rx + P * n + p);
-                        unit<CPLX, FC>(A, n, w, f0, nf, txd, txa, rxd, rxa, acc);
-                    }
+        if (MODE == USTB_DIM_RECEIVE || MODE == USTB_DIM_BOTH) {
+            if (MODE == USTB_DIM_BOTH) acc[0].zero();
+            for (int64_t w0 = 0; w0 < A.W; w0 += WC) {
+                const int wc = (int)min((int64_t)WC, A.W - w0);
+                load_tx(w0, wc);
+                if (MODE == USTB_DIM_RECEIVE)
+#pragma unroll
+                    for (int k = 0; k < WC; ++k) acc[k].zero();
+                for (int64_t n = 0; n < A.N; ++n) {
+                    const float rxa = __ldg(A.apo_rx + P * n + p);
+                    if (rxa == 0.0f) continue;
+                    const float rxd = __ldg(A.d_rx + P * n + p);
+                    chunk_units<CPLX, FC, PER_WAVE, NACC>(A, n, w0, wc, f0, nf, txd, txa, rxd, rxa, acc);
                 }
-                store<CPLX, FC>(A, p + A.w_f * w, f0, nf, acc);
+                if (MODE == USTB_DIM_RECEIVE)
+#pragma unroll
+                    for (int k = 0; k < WC; ++k)
+                        if (k < wc) store<CPLX, FC>(A, p + A.w_f * (w0 + k), f0, nf, acc[k]);
             }
+            if (MODE == USTB_DIM_BOTH) store<CPLX, FC>(A, p, f0, nf, acc[0]);
         } else {
-            if (MODE == USTB_DIM_BOTH) acc.zero();
             for (int64_t n = 0; n < A.N; ++n) {
                 const float rxa = __ldg(A.apo_rx + P * n + p);
                 const float rxd = __ldg(A.d_rx + P * n + p);
-                if (MODE == USTB_DIM_TRANSMIT) acc.zero();
-                if (rxa != 0.0f || MODE == USTB_DIM_NONE) {
-                    for (int64_t w = 0; w < A.W; ++w) {
-                        const float txa = __ldg(A.apo_tx + P * w + p);
-                        if (MODE == USTB_DIM_NONE) acc.zero();
-                        if (txa != 0.0f && rxa != 0.0f) {
-                            const float txd = __ldg(A.d_tx + P * w + p);
-                            unit<CPLX, FC>(A, n, w, f0, nf, txd, txa, rxd, rxa, acc);
-                        }
-                        if (MODE == USTB_DIM_NONE) store<CPLX, FC>(A, p + A.rx_f * n + A.w_f * w, f0, nf, acc);
-                    }
+                if (MODE == USTB_DIM_TRANSMIT) acc[0].zero();
+                for (int64_t w0 = 0; w0 < A.W; w0 += WC) {
+                    const int wc = (int)min((int64_t)WC, A.W - w0);
+                    load_tx(w0, wc);
+                    if (MODE == USTB_DIM_NONE)
+#pragma unroll
+                        for (int k = 0; k < WC; ++k) acc[k].zero();
+                    if (rxa != 0.0f)
+                        chunk_units<CPLX, FC, PER_WAVE, NACC>(A, n, w0, wc, f0, nf, txd, txa, rxd, rxa, acc);
+                    if (MODE == USTB_DIM_NONE)
+#pragma unroll
+                        for (int k = 0; k < WC; ++k)
+                            if (k < wc) store<CPLX, FC>(A, p + A.rx_f * n + A.w_f * (w0 + k), f0, nf, acc[k]);
                 }
-                if (MODE == USTB_DIM_TRANSMIT) store<CPLX, FC>(A, p + A.rx_f * n, f0, nf, acc);
+                if (MODE == USTB_DIM_TRANSMIT) store<CPLX, FC>(A, p + A.rx_f * n, f0, nf, acc[0]);
             }
-            if (MODE == USTB_DIM_BOTH) store<CPLX, FC>(A, p, f0, nf, acc);
         }
     }
 }

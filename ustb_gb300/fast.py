@@ -152,6 +152,31 @@ def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SP
     return _pack(blocks)
 
 
+def refine_tiles(tiles: np.ndarray, xyz: np.ndarray, tx_samples: np.ndarray,
+                 span_limit: float = SPAN_LIMIT) -> np.ndarray:
+    """Split tiles whose tabulated transmit delays ([P, W], in samples) span more
+    than ``span_limit`` over the tile (e.g. across the discontinuity of the hybrid
+    focused-wave model at the edges of its focal band)."""
+    out = []
+    stack = [t[t >= 0] for t in tiles]
+    while stack:
+        b = stack.pop()
+        if b.size == 0:
+            continue
+        td = tx_samples[b]
+        span = float(np.max(td.max(axis=0) - td.min(axis=0))) if b.size > 1 else 0.0
+        if span <= span_limit or b.size == 1:
+            out.append(b)
+            continue
+        ext = xyz[b].max(0) - xyz[b].min(0)
+        ax = int(np.argmax(ext))
+        order = b[np.argsort(xyz[b, ax], kind="stable")]
+        h = order.size // 2
+        stack.append(order[:h])
+        stack.append(order[h:])
+    return _pack(out)
+
+
 def _pack(blocks) -> np.ndarray:
     T = len(blocks)
     tiles = np.full((T, TILE), -1, dtype=np.int32)
@@ -232,6 +257,9 @@ class FastGeometry:
             td = geometry.transmit_delay(self.sequence, scan, model, pw_margin, blending_power,
                                          tx.f_number).astype(np.float32)
             self.d_txdelay = f32(td.T)
+            if tiles is None:
+                self.tiles = refine_tiles(self.tiles, scan.xyz, td[:, table_waves].astype(np.float64) * fs)
+                self.d_tiles = torch.from_numpy(self.tiles).to(dev)
         self.d_txapo = None
         if tx_const is None:
             self.d_txapo = f32(tx.wave_apodization(self.sequence, scan).T)
