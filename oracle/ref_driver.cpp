@@ -1,6 +1,8 @@
 /*
- * C-ABI driver around the reference's own das_c MEX function
- * (+mex/source/das_c.cpp, compiled unmodified against oracle/shim/).
+ * C-ABI driver around a MEX function with das_c's argument layout: the
+ * reference's own das_c (+mex/source/das_c.cpp, compiled unmodified against
+ * oracle/shim/), or — compiled with -DMEX_RUN_NAME=... by the tests — the
+ * product's MEX gateway, so that the MATLAB boundary is exercised without MATLAB.
  * TEST INFRASTRUCTURE ONLY: linked into oracle/_ref/libdas_c_ref.so, which the
  * tests use to pin the oracle port and to make golden fixtures.  The product
  * library never links or loads it.
@@ -46,7 +48,11 @@ static mxArray wrap(void* data, std::initializer_list<mwSize> dims, mxClassID cl
     return a;
 }
 
-extern "C" int das_c_ref_run(const float* ch, int64_t L, int64_t N, int64_t W, int64_t F,
+#ifndef MEX_RUN_NAME
+#define MEX_RUN_NAME das_c_ref_run
+#endif
+
+extern "C" int MEX_RUN_NAME(const float* ch, int64_t L, int64_t N, int64_t W, int64_t F,
                              float fs, float t0, const float* apo_tx, const float* apo_rx,
                              const float* delay_tx, const float* delay_rx, int64_t P, float fd,
                              int32_t dim, float* out, char* errbuf, int errlen) {
