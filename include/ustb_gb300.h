@@ -91,6 +91,36 @@ int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64_t L, int64
 
 
 /*
+ * Allocation-free form of ustb_das_table_f32_host.  No counterpart in the
+ * reference: das_cuda (+mex/source/das_cuda.cu:190-220) and
+ * ustb_das_table_f32_host both obtain device memory per call.
+ *
+ * For callers that must not allocate device memory while they run.  Examples
+ * are acquisition or serving loops with a hard latency budget (cudaMalloc can
+ * block and synchronise the device), and host applications that keep a fixed
+ * memory budget or let another allocator own the GPU (a MATLAB or PyTorch
+ * process with a caching pool), where a fresh cudaMalloc may fail or evict.
+ *
+ * Same arguments and result as ustb_das_table_f32_host.  The device staging
+ * buffers (channel data, the four tables and the output, each rounded up to
+ * 256 bytes) come from one static device array of USTB_NOALLOC_SCRATCH_BYTES
+ * that every GPU which loads this library holds until the process exits.
+ * Requests that need more are rejected with USTB_E_SHAPE before any copy.
+ * The call makes no cudaMalloc/cudaFree and uses the per-thread default stream.
+ * Its first call on a device looks up the array's device address (set-up, once
+ * per device); make that first call before any stream capture on that device.
+ * All calls share the one array and nothing in it is cleared (every byte used is
+ * rewritten by the call): calls that overlap on the GPU, e.g. from two host
+ * threads on one device, race on it and must be serialised by the caller.
+ */
+#define USTB_NOALLOC_SCRATCH_BYTES (64u << 20)
+int ustb_das_table_f32_host_noalloc(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
+                                    int64_t W, int64_t F, float fs, float t0, const float* apo_tx,
+                                    const float* apo_rx, const float* delay_tx,
+                                    const float* delay_rx, int64_t P, float fd, int32_t dimension,
+                                    void* out, int32_t device);
+
+/*
  * Per-pixel phase epilogue: data[p + P*j] *= phase[p] for j < rest
  * (interleaved complex single).  Replaces the MATLAB step
  * bf .* exp(-1j*2*w0*scan.reference_distance/c) at +midprocess/das.m:306-309;

@@ -12,6 +12,8 @@
 // Loop order: for dimension.both/.receive, chunks of WC waves outer (their tx
 // values in registers) and channels inner (rx values re-read once per chunk);
 // for .transmit/.none, channels outer and wave chunks inner.
+#include <mutex>
+
 #include "common.cuh"
 #include "phasor.cuh"
 
@@ -307,5 +309,83 @@ extern "C" int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64
     cudaStreamDestroy(s);
     if (rc) return rc;
     if (e != cudaSuccess) return ustb::cuda_fail(e, "host-pointer DAS copy/sync", __FILE__, __LINE__);
+    return USTB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free form of the host-pointer entry point.
+//
+// Staging buffers live in one file-scope device array instead of memory from
+// cudaMalloc.  Host code may not use the array's name as a device address, so
+// its address is looked up once per device with cudaGetSymbolAddress (with that
+// device current) and cached.  All calls share the array.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[USTB_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// The scratch array's device address on the current device `device`.
+int noalloc_scratch(int device, void** out) {
+    USTB_REQUIRE(device >= 0 && device < kMaxDevices, USTB_E_ARG, "device %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return ustb::cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return USTB_OK;
+}
+
+}  // namespace
+
+extern "C" int ustb_das_table_f32_host_noalloc(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
+                                               int64_t W, int64_t F, float fs, float t0,
+                                               const float* apo_tx, const float* apo_rx,
+                                               const float* delay_tx, const float* delay_rx, int64_t P,
+                                               float fd, int32_t dimension, void* out, int32_t device) {
+    ustb::clear_error();
+    int rc = check_table_args(ch, ch_complex, L, N, W, F, fd, dimension, apo_tx, apo_rx, delay_tx,
+                              delay_rx, P, out);
+    if (rc) return rc;
+    const size_t el = ch_complex ? 8 : 4;
+    const size_t ch_bytes = (size_t)(L * N * W * F) * el;
+    const size_t tx_bytes = (size_t)(P * W) * 4, rx_bytes = (size_t)(P * N) * 4;
+    const size_t out_bytes = (size_t)out_elems(dimension, P, N, W, F) * el;
+    auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t total = align(ch_bytes) + 2 * align(tx_bytes) + 2 * align(rx_bytes) + align(out_bytes);
+    USTB_REQUIRE(total <= (size_t)USTB_NOALLOC_SCRATCH_BYTES, USTB_E_SHAPE,
+                 "this request needs %zu bytes of device scratch; the allocation-free entry point has "
+                 "%zu (USTB_NOALLOC_SCRATCH_BYTES): use ustb_das_table_f32_host or split the pixels",
+                 total, (size_t)USTB_NOALLOC_SCRATCH_BYTES);
+    USTB_CUDA(cudaSetDevice(device));
+    void* scratch = nullptr;
+    rc = noalloc_scratch(device, &scratch);
+    if (rc) return rc;
+    char* p = static_cast<char*>(scratch);
+    void* d_ch = p; p += align(ch_bytes);
+    float* d_atx = (float*)p; p += align(tx_bytes);
+    float* d_dtx = (float*)p; p += align(tx_bytes);
+    float* d_arx = (float*)p; p += align(rx_bytes);
+    float* d_drx = (float*)p; p += align(rx_bytes);
+    void* d_out = p;
+    // Every staged byte is overwritten below and the kernel writes every output
+    // element, so nothing in the shared array needs clearing between calls.
+    cudaStream_t s = cudaStreamPerThread;
+    if (ch_bytes) USTB_CUDA(cudaMemcpyAsync(d_ch, ch, ch_bytes, cudaMemcpyHostToDevice, s));
+    if (tx_bytes) USTB_CUDA(cudaMemcpyAsync(d_atx, apo_tx, tx_bytes, cudaMemcpyHostToDevice, s));
+    if (tx_bytes) USTB_CUDA(cudaMemcpyAsync(d_dtx, delay_tx, tx_bytes, cudaMemcpyHostToDevice, s));
+    if (rx_bytes) USTB_CUDA(cudaMemcpyAsync(d_arx, apo_rx, rx_bytes, cudaMemcpyHostToDevice, s));
+    if (rx_bytes) USTB_CUDA(cudaMemcpyAsync(d_drx, delay_rx, rx_bytes, cudaMemcpyHostToDevice, s));
+    rc = ustb_das_table_f32(d_ch, ch_complex, L, N, W, F, fs, t0, d_atx, d_arx, d_dtx, d_drx, P, fd,
+                            dimension, d_out, s);
+    if (rc) return rc;
+    if (out_bytes) USTB_CUDA(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s));
+    USTB_CUDA(cudaStreamSynchronize(s));
     return USTB_OK;
 }
