@@ -242,6 +242,15 @@ int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L
 int ustb_convert_channels(const void* src, int32_t src_type, void* dst, int32_t dst_type,
                           int64_t count, float scale, void* stream);
 
+/*
+ * FIR filter along depth with delay compensation, for the band-pass step of the
+ * simplified-DMAS post-process (+postprocess/simplified_delay_multiply_and_sum.m:170-176):
+ * out[c][z] = sum_k taps[k] * in[c][z + delay - k], zero outside [0, nz).
+ * in/out: ncols columns of nz real samples each (depth fastest).  Device pointers.
+ */
+int ustb_fir_depth(const float* in, float* out, int64_t nz, int64_t ncols, const float* taps,
+                   int32_t ntaps, int32_t delay, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -181,3 +181,15 @@ def sdmas_value(s_real):
     root = (np.sign(s) * np.sqrt(np.abs(s))).sum(axis=1, keepdims=True)
     absum = np.abs(s).sum(axis=1, keepdims=True)
     return (root ** 2 - absum) / 2.0
+
+
+def sdmas_filtered(y, taps):
+    """Band-pass along axis 0 with delay compensation and Hilbert transform
+    (simplified_delay_multiply_and_sum.m:170-192): y real [Nz, ...]."""
+    from scipy.signal import hilbert, lfilter
+
+    y = np.asarray(y, np.float64)
+    d = int(round((len(taps) - 1) / 2))
+    pad = np.concatenate([y, np.zeros((d,) + y.shape[1:])], axis=0)
+    f = lfilter(taps, 1.0, pad, axis=0)[d:]
+    return hilbert(f, axis=0)

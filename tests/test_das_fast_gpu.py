@@ -238,3 +238,44 @@ def test_tile_planner_bounds_the_window():
         assert np.linalg.norm(xyz.max(0) - xyz.min(0)) <= lim + 1e-12
     # most lanes are busy
     assert live.mean() > 0.6
+
+
+def test_sdmas_bandpass_and_hilbert_follow_up(cuda_dev):
+    """The fused per-pixel sDMAS value, band-passed along depth around 2*f0 and made
+    analytic (simplified_delay_multiply_and_sum.m:151-192), against the FP64 chain."""
+    from ustb_gb300 import postprocess
+
+    rng = np.random.default_rng(11)
+    N, L, W = 24, 768, 3
+    probe = Probe.linear_array(N, 0.3e-3)
+    fs, f0, c = 20e6, 5e6, 1540.0
+    seq = [Wave.plane(a) for a in np.deg2rad([-5.0, 0.0, 5.0])]
+    nz, nx = 160, 24
+    z = np.linspace(6e-3, 12e-3, nz)
+    scan = LinearScan(np.linspace(-2e-3, 2e-3, nx), z)
+    ch = smooth(speckle(rng, (L, N, W, 1)))
+    rx = Apodization(window=Window.boxcar, f_number=1.0)
+    ref, _ = oracle_f64(ch, fs, 0.0, f0, c, probe, scan, seq, 2, rx, Apodization())
+    ph = np.exp(-1j * 4 * np.pi * f0 * scan.reference_distance / c)
+    g = fast.FastGeometry(probe, scan, seq, fs, 0.0, f0, c, cuda_dev, rx, None, pixel_phase=ph)
+    dev_ch = torch.from_numpy(np.ascontiguousarray(ch.transpose(3, 2, 1, 0))).to(cuda_dev)
+    st = fast.convert_channels(dev_ch, Precision.fp32)
+    outs = fast.das_fast(st, Precision.fp32, True, g, Dimension.transmit, epilogue=True, cube=False, L=L)
+    dz = float(np.mean(np.diff(z)))
+    img = postprocess.simplified_dmas_image(outs["sdmas"], nz, nx, dz, c, f0=f0 / 4)
+    taps = postprocess.bandpass_taps([1.5 * f0 / 4, 1.5 * f0 / 4 + f0 / 16, 2.5 * f0 / 4, 2.5 * f0 / 4 + f0 / 16],
+                                     c / dz / 2)
+    sd = O.sdmas_value(ref[:, :, 0, :].real)[:, 0, 0].reshape(nx, nz).T
+    want = O.sdmas_filtered(sd, taps).T.reshape(-1)
+    got = img.cpu().numpy()[0]
+    assert rel_l2(got, want) <= 2e-3
+
+
+def test_kaiser_design_matches_kaiser_formulas():
+    from ustb_gb300.postprocess import bandpass_taps, kaiser_order
+
+    n, Wn, beta = kaiser_order([7.5e6, 8.75e6, 12.5e6, 13.75e6], [1e-3] * 3, 1540 / 0.05e-3 / 2)
+    assert beta == pytest.approx(0.1102 * (60 - 8.7))
+    assert n == math.ceil((60 - 7.95) / (2 * math.pi * 2.285 * (1.25e6 / (1540 / 0.05e-3 / 2))))
+    taps = bandpass_taps([7.5e6, 8.75e6, 12.5e6, 13.75e6], 1540 / 0.05e-3 / 2)
+    assert taps.size == n + 1 and np.allclose(taps, taps[::-1])

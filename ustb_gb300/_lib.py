@@ -32,6 +32,7 @@ SIGNATURES = {
     "ustb_apply_pixel_phase": (ctypes.c_int, [vp, i64, i64, vp, vp]),
     "ustb_das_fast": (ctypes.c_int, [vp, i32, i32, i64, i64, i64, i64, vp, i32, i32, vp, vp, vp]),
     "ustb_convert_channels": (ctypes.c_int, [vp, i32, vp, i32, i64, f32, vp]),
+    "ustb_fir_depth": (ctypes.c_int, [vp, vp, i64, i64, vp, i32, i32, vp]),
 }
 
 STATUS = {0: "USTB_OK", 1: "USTB_E_ARG", 2: "USTB_E_SHAPE", 3: "USTB_E_DTYPE", 4: "USTB_E_CUDA",

@@ -158,8 +158,8 @@ __device__ __forceinline__ float rx_apodization(const Params& A, float ex, float
     }
     const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
     const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
-    const float rt = fabsf(A.fnx * (xd / zx));
-    const float rp = fabsf(A.fny * (yd / zy));
+    const float rt = fabsf(A.fnx * __fdividef(xd, zx));
+    const float rp = fabsf(A.fny * __fdividef(yd, zy));
     return window(A.rx_window, rt) * window(A.rx_window, rp);
 }
 
@@ -269,21 +269,91 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// bytes per stored sample
+template <int ST, bool CPLX>
+struct StoreInfo {
+    static constexpr int bytes = (ST == USTB_STORE_F32 ? 4 : 2) * (CPLX ? 2 : 1);
+};
+
+// a raw staged sample (shared memory) as float2
+template <int ST, bool CPLX>
+__device__ __forceinline__ float2 raw_sample(const unsigned char* raw, int i) {
+    if constexpr (CPLX) {
+        if constexpr (ST == USTB_STORE_F32) return reinterpret_cast<const float2*>(raw)[i];
+        else if constexpr (ST == USTB_STORE_F16) return __half22float2(reinterpret_cast<const __half2*>(raw)[i]);
+        else return __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(raw)[i]);
+    } else {
+        if constexpr (ST == USTB_STORE_F32) return make_float2(reinterpret_cast<const float*>(raw)[i], 0.f);
+        else if constexpr (ST == USTB_STORE_F16) return make_float2(__half2float(reinterpret_cast<const __half*>(raw)[i]), 0.f);
+        else return make_float2(__bfloat162float(reinterpret_cast<const __nv_bfloat16*>(raw)[i]), 0.f);
+    }
+}
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+constexpr int kRawSamples = kSlot + 16;  // window + 1 + alignment slack
+
+// Conservative test that channel `n`'s receive window is zero over the whole tile
+// box: every window is 0 for ratio > 1/2 (apodization.m:172-186), and the ratio
+// F#*|x_dist|/|z| is bounded below by the box.
+__device__ __forceinline__ bool rx_active(const Params& A, const Box& b, float ex, float ey, float ez) {
+    if (A.rx_apo_tab || A.rx_window == USTB_WIN_NONE) return true;
+    float xd, yd, zmax;
+    if (A.rx_origin) {
+        xd = fabsf(ex - A.ox);
+        yd = fabsf(ey - A.oy);
+        float dmin, dmax;
+        dist_range(b, A.ox, A.oy, A.oz, dmin, dmax);
+        zmax = dmax;
+    } else {
+        xd = fmaxf(0.f, fmaxf(b.lo[0] - ex, ex - b.hi[0]));
+        yd = fmaxf(0.f, fmaxf(b.lo[1] - ey, ey - b.hi[1]));
+        zmax = fmaxf(fabsf(b.lo[2] - ez), fabsf(b.hi[2] - ez));
+    }
+    const float zx = fminf(fmaxf(zmax, A.minx * A.fnx), A.maxx * A.fnx);
+    const float zy = fminf(fmaxf(zmax, A.miny * A.fny), A.maxy * A.fny);
+    if (!(zx > 0.f) || !(zy > 0.f)) return true;
+    const float lim = 0.5f * (1.f + 1e-4f);
+    return !(A.fnx * xd / zx > lim || A.fny * yd / zy > lim);
+}
+
+template <bool CPLX, int ST>
+struct CtasPerSm {
+    static constexpr int value = (CPLX && ST == USTB_STORE_F32) ? 1 : 2;
+};
+
 template <int MODE, bool CPLX, int ST, bool EPI>
-__global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
+__global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_kernel(const Params A) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
     constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
     constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
-    constexpr int NS = CG * KW;
+    constexpr int NS = CG * KW;           // slots per stage
+    constexpr int SB = StoreInfo<ST, CPLX>::bytes;
+    constexpr int SPC = 16 / SB;          // samples per 16-byte chunk
+    constexpr int RAWB = kRawSamples * SB;
+    constexpr int MAXCH = RAWB / 16;
     using Entry = typename EntryT<CPLX>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Entry* slots = reinterpret_cast<Entry*>(smem_raw);
-    __shared__ int s_base_n[CG], s_base_w[KW];
-    __shared__ int s_len_n[CG], s_len_w[KW];  // ceil(upper bound - base) per component
-    __shared__ int s_act_n[CG], s_act_w[KW];
+    static_assert(RAWB % 16 == 0, "raw slot must be a whole number of 16-byte chunks");
+
+    const int64_t L = A.L, N = A.N, W = A.W, P = A.P;
+    extern __shared__ __align__(16) unsigned char smem[];
+    Entry* slots = reinterpret_cast<Entry*>(smem);
+    unsigned char* raw_base = smem + (size_t)NS * kSlot * sizeof(Entry);
+    int* base_n = reinterpret_cast<int*>(raw_base + 2 * NS * RAWB);
+    int* len_n = base_n + N;
+    int* base_w = len_n + N;
+    int* len_w = base_w + W;
+    unsigned char* act_n = reinterpret_cast<unsigned char*>(len_w + W);
+    unsigned char* act_w = act_n + N;
     __shared__ float2 s_red[kTile / 32];
 
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     const int64_t f = blockIdx.y;
     const int32_t* tl = A.tiles + (int64_t)blockIdx.x * kTile;
     const int32_t p_own = __ldg(tl + tid);
@@ -291,87 +361,212 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
     const int64_t p = live ? p_own : __ldg(tl);
     const float px = __ldg(A.px + 3 * p), py = __ldg(A.px + 3 * p + 1), pz = __ldg(A.px + 3 * p + 2);
 
-    // tile bounding box
     Box box;
     {
         const float big = 3.4e38f;
-        float2 r;
-        r = block_minmax(live ? px : big, live ? px : -big, s_red);
+        float2 r = block_minmax(live ? px : big, live ? px : -big, s_red);
         box.lo[0] = r.x; box.hi[0] = r.y;
         r = block_minmax(live ? py : big, live ? py : -big, s_red);
         box.lo[1] = r.x; box.hi[1] = r.y;
         r = block_minmax(live ? pz : big, live ? pz : -big, s_red);
         box.lo[2] = r.x; box.hi[2] = r.y;
     }
-    const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
-    const float fd_c = A.fd * A.inv_c;  // cycles per metre
 
-    const int64_t L = A.L, N = A.N, W = A.W, P = A.P;
-    const char* chf = reinterpret_cast<const char*>(A.ch);
-    const int64_t esz = CPLX ? (ST == USTB_STORE_F32 ? 8 : 4) : (ST == USTB_STORE_F32 ? 4 : 2);
+    // ---- per-tile window bases, lengths and activity ----------------------
+    for (int64_t n = tid; n < N; n += kTile) {
+        const float ex = __ldg(A.el + 3 * n), ey = __ldg(A.el + 3 * n + 1), ez = __ldg(A.el + 3 * n + 2);
+        float dmin, dmax;
+        dist_range(box, ex, ey, ez, dmin, dmax);
+        const float lo = (dmin * A.inv_c + A.lens) * A.fs, hi = (dmax * A.inv_c + A.lens) * A.fs;
+        const float base = floorf(lo) - 1.f;
+        const bool ok = (hi - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
+        const bool act = rx_active(A, box, ex, ey, ez);
+        if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
+        base_n[n] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        len_n[n] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
+        act_n[n] = act ? 1 : 0;
+    }
+    for (int64_t w = tid; w < W; w += kTile) {
+        const ustb_wave wv = A.waves[w];
+        if (wv.kind == USTB_WAVE_TABLE) continue;
+        float lo, hi;
+        tx_tau_range(wv, box, lo, hi);
+        lo = (lo - A.t0) * A.fs;
+        hi = (hi - A.t0) * A.fs;
+        const float base = floorf(lo) - 1.f;
+        const bool ok = (hi - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
+        const bool act = A.tx_apo_tab != nullptr || wv.apodization != 0.f;
+        if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
+        base_w[w] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        len_w[w] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
+        act_w[w] = act ? 1 : 0;
+    }
+    if (A.tx_delay_tab) {  // tabulated transmit delays: the tile's actual range
+        for (int64_t w = 0; w < W; ++w) {
+            if (A.waves[w].kind != USTB_WAVE_TABLE) continue;
+            const float s = (__ldg(A.tx_delay_tab + w * P + p) - A.t0) * A.fs;
+            const float2 r = block_minmax(live ? s : 3.4e38f, live ? s : -3.4e38f, s_red);
+            if (tid == 0) {
+                const float base = floorf(r.x) - 1.f;
+                const bool ok = (r.y - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
+                if (!ok) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
+                base_w[w] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                len_w[w] = (int)fminf(fmaxf(ceilf(r.y - base), 0.f), kHalf);
+                act_w[w] = 1;
+            }
+        }
+    }
+    __syncthreads();
+
+    const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
+    const float fd_c = A.fd * A.inv_c;
+    const char* chb = reinterpret_cast<const char*>(A.ch);
+    const int64_t TOT = L * N * W * A.F;  // samples in the whole array
     const int64_t frame_off = f * W * N * L;
 
-    // per-thread state
+    auto group_active = [&](int64_t n0) {
+        bool a = false;
+#pragma unroll
+        for (int c = 0; c < CG; ++c) a |= (n0 + c < N) && act_n[n0 + c];
+        return a;
+    };
+    auto chunk_active = [&](int64_t w0) {
+        bool a = false;
+#pragma unroll
+        for (int k = 0; k < KW; ++k) a |= (w0 + k < W) && act_w[w0 + k];
+        return a;
+    };
+    // next active stage after (o, i) in loop order: outer index o, inner i
+    const int64_t OUTS = ORDER_A ? KW : CG, INS = ORDER_A ? CG : KW;
+    const int64_t OUTN = ORDER_A ? W : N, INN = ORDER_A ? N : W;
+    auto stage_active = [&](int64_t o, int64_t i) {
+        return ORDER_A ? (chunk_active(o) && group_active(i)) : (group_active(o) && chunk_active(i));
+    };
+    auto advance = [&](int64_t& o, int64_t& i) -> bool {
+        for (;;) {
+            i += INS;
+            if (i >= INN) { i = 0; o += OUTS; }
+            if (o >= OUTN) return false;
+            if (stage_active(o, i)) return true;
+        }
+    };
+
+    // issue the raw copies of stage (w0, n0) into buffer b
+    auto issue = [&](int64_t w0, int64_t n0, int b) {
+        unsigned char* rb = raw_base + b * NS * RAWB;
+        for (int slot = warp; slot < NS; slot += kTile / 32) {
+            const int c = slot / KW, k = slot - c * KW;
+            const int64_t n = n0 + c, w = w0 + k;
+            if (n >= N || w >= W || !act_n[n] || !act_w[w]) continue;
+            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
+            const int64_t g0 = frame_off + (w * N + n) * L + base_n[n] + base_w[w];
+            const int64_t ga = g0 >= 0 ? (g0 / SPC) * SPC : -(((-g0) + SPC - 1) / SPC) * SPC;
+            const int nch = (int)((g0 - ga + len + 1 + SPC - 1) / SPC);
+            unsigned char* dst = rb + slot * RAWB;
+            for (int ch = lane; ch < nch && ch < MAXCH; ch += 32) {
+                const int64_t cs = ga + (int64_t)ch * SPC;
+                if (cs >= 0 && cs + SPC <= TOT) {
+                    cp_async16(dst + ch * 16, chb + cs * SB);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < SPC; ++e) {
+                        const int64_t idx = cs + e;
+#pragma unroll
+                        for (int by = 0; by < SB; ++by)
+                            dst[ch * 16 + e * SB + by] = (idx >= 0 && idx < TOT) ? (unsigned char)chb[idx * SB + by] : 0;
+                    }
+                }
+            }
+        }
+        cp_async_commit();
+    };
+
+    // raw samples -> interpolation entries {x_i, x_{i+1} - x_i} with das_c's validity rule
+    auto transform = [&](int64_t w0, int64_t n0, int b) {
+        const unsigned char* rb = raw_base + b * NS * RAWB;
+        for (int slot = warp; slot < NS; slot += kTile / 32) {
+            const int c = slot / KW, k = slot - c * KW;
+            const int64_t n = n0 + c, w = w0 + k;
+            if (n >= N || w >= W || !act_n[n] || !act_w[w]) {
+                // units of this slot carry zero weight and read j <= kHalf: make those zeros
+                Entry* dz = slots + slot * kSlot;
+                for (int j = lane; j <= (int)kHalf; j += 32) {
+                    if constexpr (CPLX) dz[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    else dz[j] = make_float2(0.f, 0.f);
+                }
+                continue;
+            }
+            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
+            const int64_t i0 = (int64_t)base_n[n] + base_w[w];
+            const int64_t g0 = frame_off + (w * N + n) * L + i0;
+            const int64_t ga = g0 >= 0 ? (g0 / SPC) * SPC : -(((-g0) + SPC - 1) / SPC) * SPC;
+            const int off = (int)(g0 - ga);
+            const unsigned char* src = rb + slot * RAWB;
+            Entry* dst = slots + slot * kSlot;
+            for (int j = lane; j < len; j += 32) {
+                const int64_t i = i0 + j;
+                Entry v;
+                if constexpr (CPLX) v = make_float4(0.f, 0.f, 0.f, 0.f);
+                else v = make_float2(0.f, 0.f);
+                if (i >= 1 && i <= L - 2) {
+                    const float2 x0 = raw_sample<ST, CPLX>(src, off + j);
+                    const float2 x1 = raw_sample<ST, CPLX>(src, off + j + 1);
+                    if constexpr (CPLX) v = make_float4(x0.x, x0.y, x1.x - x0.x, x1.y - x0.y);
+                    else v = make_float2(x0.x, x1.x - x0.x);
+                }
+                dst[j] = v;
+            }
+        }
+    };
+
+    // per-thread geometry
     float srx[CG];
     float2 B[CG];
     float rxapo[CG];
     float stx[KW];
     float2 Aw[KW];
-    float accr[ORDER_A ? KW : CG], acci[ORDER_A ? KW : CG];
-    float2 Y = make_float2(0.f, 0.f);  // dimension.both
-    // epilogue accumulators
+    constexpr int NACC = ORDER_A ? KW : CG;
+    float accr[NACC], acci[NACC];
+    float2 Y = make_float2(0.f, 0.f);
     float2 eS = make_float2(0.f, 0.f);
     float eI = 0.f, eM = 0.f, eR = 0.f, eQ = 0.f;
 
-    auto setup_rx = [&](int64_t n0, int cg) {
+    auto setup_rx = [&](int64_t n0) {
 #pragma unroll
         for (int c = 0; c < CG; ++c) {
             const int64_t n = n0 + c;
             float s = 0.f, apo = 0.f;
-            float2 b = make_float2(0.f, 0.f);
-            if (c < cg) {
+            float2 bb = make_float2(0.f, 0.f);
+            if (n < N && act_n[n]) {
                 const float ex = __ldg(A.el + 3 * n), ey = __ldg(A.el + 3 * n + 1), ez = __ldg(A.el + 3 * n + 2);
                 const float dx = px - ex, dy = py - ey, dz = pz - ez;
-                const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-                const float tau = r * A.inv_c + A.lens;
-                s = tau * A.fs;
+                const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-30f);
+                const float r = r2 * rsqrtf(r2);
+                s = (r * A.inv_c + A.lens) * A.fs - (float)base_n[n];
                 apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
                 if (!live) apo = 0.f;
                 if (CPLX) {
                     const float2 e = phasor_cycles(r * fd_c + A.lens * A.fd);
-                    b = make_float2(apo * e.x, apo * e.y);
+                    bb = make_float2(apo * e.x, apo * e.y);
                 } else {
-                    b = make_float2(apo, 0.f);
-                }
-                if (tid == 0) {
-                    float dmin, dmax;
-                    dist_range(box, ex, ey, ez, dmin, dmax);
-                    const float lo = (dmin * A.inv_c + A.lens) * A.fs, hi = (dmax * A.inv_c + A.lens) * A.fs;
-                    const float base = floorf(lo) - 1.f;
-                    if (!(hi - base <= kHalf - 2.f) || !(fabsf(base) < 1.0e9f)) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-                    s_base_n[c] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
-                    s_len_n[c] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
+                    bb = make_float2(apo, 0.f);
                 }
             }
-            srx[c] = s;
-            B[c] = b;
+            srx[c] = fminf(fmaxf(s, 0.f), kHalf);  // NaN -> kHalf: stays inside the slot
+            B[c] = bb;
             rxapo[c] = apo;
-            const int any = __syncthreads_or(apo != 0.f);
-            if (tid == 0) s_act_n[c] = (c < cg) && any;
         }
     };
-
-    auto setup_tx = [&](int64_t w0, int kw) {
-        // table-driven delays need the tile's actual range
+    auto setup_tx = [&](int64_t w0) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) {
             const int64_t w = w0 + k;
             float s = 0.f, apo = 0.f;
             float2 a = make_float2(0.f, 0.f);
-            if (k < kw) {
+            if (w < W && act_w[w]) {
                 const ustb_wave wv = A.waves[w];
                 const float tau = tx_tau(A, wv, w, p, px, py, pz);
-                s = (tau - A.t0) * A.fs;
+                s = (tau - A.t0) * A.fs - (float)base_w[w];
                 apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + w * P + p) : wv.apodization;
                 if (!live) apo = 0.f;
                 if (CPLX) {
@@ -380,101 +575,77 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
                 } else {
                     a = make_float2(apo, 0.f);
                 }
-                float lo, hi;
-                if (wv.kind == USTB_WAVE_TABLE) {
-                    const float2 r = block_minmax(live ? s : 3.4e38f, live ? s : -3.4e38f, s_red);
-                    lo = r.x; hi = r.y;
-                } else {
-                    tx_tau_range(wv, box, lo, hi);
-                    lo = (lo - A.t0) * A.fs;
-                    hi = (hi - A.t0) * A.fs;
-                }
-                if (tid == 0) {
-                    const float base = floorf(lo) - 1.f;
-                    if (!(hi - base <= kHalf - 2.f) || !(fabsf(base) < 1.0e9f)) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-                    s_base_w[k] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
-                    s_len_w[k] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
-                }
             }
-            stx[k] = s;
+            stx[k] = fminf(fmaxf(s, 0.f), kHalf);
             Aw[k] = a;
-            const int any = __syncthreads_or(apo != 0.f);
-            if (tid == 0) s_act_w[k] = (k < kw) && any;
         }
     };
 
-    // convert absolute delays to window-relative, clamped into [0, kHalf]
-    // (NaN and out-of-window values end up inside the slot; overflow is flagged)
-    auto localise_rx = [&]() {
-        __syncthreads();  // s_base_n visible
-#pragma unroll
-        for (int c = 0; c < CG; ++c) srx[c] = fminf(fmaxf(srx[c] - (float)s_base_n[c], 0.f), kHalf);
-    };
-    auto localise_tx = [&]() {
-        __syncthreads();  // s_base_w visible
-#pragma unroll
-        for (int k = 0; k < KW; ++k) stx[k] = fminf(fmaxf(stx[k] - (float)s_base_w[k], 0.f), kHalf);
-    };
-
-    // Stage the windows of (channel group n0, wave chunk w0): one warp per slot,
-    // only the entries the tile can reach (len = spans + margin, <= kSlot).
-    auto stage_fill = [&](int64_t n0, int64_t w0) {
-        __syncthreads();  // previous stage consumed
-        const int warp = tid >> 5, lane = tid & 31;
-        for (int slot = warp; slot < NS; slot += kTile / 32) {
-            const int c = slot / KW, k = slot - c * KW;
-            if (!(s_act_n[c] && s_act_w[k])) continue;
-            const int len = min(kSlot, s_len_n[c] + s_len_w[k] + 3);
-            const int64_t i0 = (int64_t)s_base_n[c] + s_base_w[k];
-            const int64_t tb = frame_off + ((w0 + k) * N + (n0 + c)) * L;
-            Entry* dst = slots + slot * kSlot;
-            for (int j = lane; j < len; j += 32) {
-                const int64_t i = i0 + j;
-                Entry v;
-                if constexpr (CPLX) v = make_float4(0.f, 0.f, 0.f, 0.f);
-                else v = make_float2(0.f, 0.f);
-                if (i >= 1 && i <= L - 2) {
-                    const float2 x0 = Sample<ST, CPLX>::load(chf, tb + i);
-                    const float2 x1 = Sample<ST, CPLX>::load(chf, tb + i + 1);
-                    if constexpr (CPLX) v = make_float4(x0.x, x0.y, x1.x - x0.x, x1.y - x0.y);
-                    else v = make_float2(x0.x, x1.x - x0.x);
-                }
-                dst[j] = v;
-            }
-        }
-        __syncthreads();
-    };
-
-    // one unit: interpolated sample of slot (c, k) at relative delay s
+    // shared address of entry 0 of slot 0, minus the bias of the 2^23 floor trick
+    const unsigned slot0 = (unsigned)__cvta_generic_to_shared(slots) - (unsigned)kMagicBits * (unsigned)sizeof(Entry);
     auto interp = [&](int c, int k, float s) -> float2 {
         const float t = __fadd_rz(s, kMagic);
-        const int j = __float_as_int(t) - kMagicBits;
         const float b = s - (t - kMagic);
-        const Entry e = slots[(c * KW + k) * kSlot + j];
-        if constexpr (CPLX) return make_float2(fmaf(b, e.z, e.x), fmaf(b, e.w, e.y));
-        else return make_float2(fmaf(b, e.y, e.x), 0.f);
+        const unsigned addr = (unsigned)__float_as_int(t) * (unsigned)sizeof(Entry) + slot0 +
+                              (unsigned)((c * KW + k) * kSlot * (int)sizeof(Entry));
+        if constexpr (CPLX) {
+            float4 e;
+            asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n"
+                         : "=f"(e.x), "=f"(e.y), "=f"(e.z), "=f"(e.w) : "r"(addr));
+            return make_float2(fmaf(b, e.z, e.x), fmaf(b, e.w, e.y));
+        } else {
+            float2 e;
+            asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(e.x), "=f"(e.y) : "r"(addr));
+            return make_float2(fmaf(b, e.y, e.x), 0.f);
+        }
     };
 
-    (void)esz;
+    auto store_cube = [&](int64_t o, float2 y) {
+        if (!live || !A.cube) return;
+        if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = y;
+        else reinterpret_cast<float*>(A.cube)[o] = y.x;
+    };
+
+    // first active stage
+    int64_t no = 0, ni = -INS;
+    bool have_next = advance(no, ni);
+    int buf = 0;
+    if (have_next) issue(ORDER_A ? no : ni, ORDER_A ? ni : no, buf);
+
+    // one pipelined stage: copies for the next stage go out before this one is used
+    auto run_stage = [&](int64_t w0, int64_t n0) {
+        int64_t o2 = no, i2 = ni;
+        const bool more = advance(o2, i2);
+        if (more) issue(ORDER_A ? o2 : i2, ORDER_A ? i2 : o2, buf ^ 1);
+        else cp_async_commit();  // keep one group per stage
+        no = o2; ni = i2;
+        cp_async_wait_prev();
+        __syncthreads();  // raw(s) visible everywhere; previous stage's entries consumed
+        transform(w0, n0, buf);
+        __syncthreads();
+        buf ^= 1;
+    };
+
     if constexpr (ORDER_A) {
         for (int64_t w0 = 0; w0 < W; w0 += KW) {
             const int kw = (int)min((int64_t)KW, W - w0);
-            setup_tx(w0, kw);
-            localise_tx();
+            if (!chunk_active(w0)) {
+                if (MODE == USTB_DIM_RECEIVE)
+                    for (int k = 0; k < kw; ++k) store_cube(p + A.w_f * (w0 + k) + A.f_f * f, make_float2(0.f, 0.f));
+                continue;
+            }
+            setup_tx(w0);
 #pragma unroll
             for (int k = 0; k < KW; ++k) accr[k] = acci[k] = 0.f;
             for (int64_t n0 = 0; n0 < N; n0 += CG) {
-                const int cg = (int)min((int64_t)CG, N - n0);
-                setup_rx(n0, cg);
-                localise_rx();
-                stage_fill(n0, w0);
+                if (!group_active(n0)) continue;
+                run_stage(w0, n0);
+                setup_rx(n0);
 #pragma unroll
                 for (int c = 0; c < CG; ++c) {
-                    if (!s_act_n[c]) continue;
                     const float2 b = B[c];
 #pragma unroll
                     for (int k = 0; k < KW; ++k) {
-                        if (!s_act_w[k]) continue;
                         const float2 v = interp(c, k, stx[k] + srx[c]);
                         if constexpr (CPLX) {
                             accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
@@ -485,7 +656,6 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
                     }
                 }
             }
-            // fold the wave chunk
 #pragma unroll
             for (int k = 0; k < KW; ++k) {
                 if (k >= kw) continue;
@@ -495,64 +665,58 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
                 if (MODE == USTB_DIM_BOTH) {
                     Y.x += y.x;
                     Y.y += y.y;
-                } else if (live && A.cube) {
-                    const int64_t o = p + A.w_f * (w0 + k) + A.f_f * f;
-                    if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = cmul(y, ph);
-                    else reinterpret_cast<float*>(A.cube)[o] = y.x;
+                } else {
+                    store_cube(p + A.w_f * (w0 + k) + A.f_f * f, CPLX ? cmul(y, ph) : y);
                 }
             }
         }
-        if (MODE == USTB_DIM_BOTH && live && A.cube) {
-            const int64_t o = p + A.f_f * f;
-            if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = cmul(Y, ph);
-            else reinterpret_cast<float*>(A.cube)[o] = Y.x;
-        }
+        if (MODE == USTB_DIM_BOTH) store_cube(p + A.f_f * f, CPLX ? cmul(Y, ph) : Y);
     } else {
         for (int64_t n0 = 0; n0 < N; n0 += CG) {
             const int cg = (int)min((int64_t)CG, N - n0);
-            setup_rx(n0, cg);
-            localise_rx();
+            if (!group_active(n0)) {
+                for (int c = 0; c < cg; ++c) {
+                    if (MODE == USTB_DIM_TRANSMIT) store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, make_float2(0.f, 0.f));
+                    if (MODE == USTB_DIM_NONE)
+                        for (int64_t w = 0; w < W; ++w)
+                            store_cube(p + A.rx_f * (n0 + c) + A.w_f * w + A.f_f * f, make_float2(0.f, 0.f));
+                }
+                continue;
+            }
+            setup_rx(n0);
 #pragma unroll
             for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
             for (int64_t w0 = 0; w0 < W; w0 += KW) {
                 const int kw = (int)min((int64_t)KW, W - w0);
-                setup_tx(w0, kw);
-                localise_tx();
-                stage_fill(n0, w0);
+                const bool ca = chunk_active(w0);
+                if (ca) {
+                    run_stage(w0, n0);
+                    setup_tx(w0);
+                }
 #pragma unroll
                 for (int c = 0; c < CG; ++c) {
-                    if (!s_act_n[c]) continue;
 #pragma unroll
                     for (int k = 0; k < KW; ++k) {
-                        if (!s_act_w[k]) continue;
-                        const float2 v = interp(c, k, stx[k] + srx[c]);
                         if (MODE == USTB_DIM_NONE) {
-                            if (live && A.cube) {
-                                const int64_t o = p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f;
-                                if constexpr (CPLX)
-                                    reinterpret_cast<float2*>(A.cube)[o] = cmul(cmul(cmul(Aw[k], B[c]), v), ph);
-                                else
-                                    reinterpret_cast<float*>(A.cube)[o] = Aw[k].x * B[c].x * v.x;
+                            const bool u = ca && (n0 + c < N) && act_n[n0 + c] && (w0 + k < W) && act_w[w0 + k];
+                            if (c < cg && k < kw) {
+                                float2 y = make_float2(0.f, 0.f);
+                                if (u) {
+                                    const float2 v = interp(c, k, stx[k] + srx[c]);
+                                    y = CPLX ? cmul(cmul(cmul(Aw[k], B[c]), v), ph) : make_float2(Aw[k].x * B[c].x * v.x, 0.f);
+                                }
+                                store_cube(p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f, y);
                             }
-                        } else if constexpr (CPLX) {
-                            accr[c] = fmaf(Aw[k].x, v.x, fmaf(-Aw[k].y, v.y, accr[c]));
-                            acci[c] = fmaf(Aw[k].x, v.y, fmaf(Aw[k].y, v.x, acci[c]));
-                        } else {
-                            accr[c] = fmaf(Aw[k].x, v.x, accr[c]);
+                        } else if (ca) {
+                            const float2 v = interp(c, k, stx[k] + srx[c]);
+                            if constexpr (CPLX) {
+                                accr[c] = fmaf(Aw[k].x, v.x, fmaf(-Aw[k].y, v.y, accr[c]));
+                                acci[c] = fmaf(Aw[k].x, v.y, fmaf(Aw[k].y, v.x, acci[c]));
+                            } else {
+                                accr[c] = fmaf(Aw[k].x, v.x, accr[c]);
+                            }
                         }
                     }
-                }
-                if (MODE == USTB_DIM_NONE && live && A.cube) {
-                    // units skipped by a zero apodization are zero, as in das_c
-#pragma unroll
-                    for (int c = 0; c < CG; ++c)
-#pragma unroll
-                        for (int k = 0; k < KW; ++k)
-                            if (c < cg && k < kw && !(s_act_n[c] && s_act_w[k])) {
-                                const int64_t o = p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f;
-                                if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = make_float2(0.f, 0.f);
-                                else reinterpret_cast<float*>(A.cube)[o] = 0.f;
-                            }
                 }
             }
             if (MODE == USTB_DIM_TRANSMIT) {
@@ -562,11 +726,7 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
                     float2 y;
                     if constexpr (CPLX) y = cmul(cmul(B[c], make_float2(accr[c], acci[c])), ph);
                     else y = make_float2(B[c].x * accr[c], 0.f);
-                    if (live && A.cube) {
-                        const int64_t o = p + A.rx_f * (n0 + c) + A.f_f * f;
-                        if constexpr (CPLX) reinterpret_cast<float2*>(A.cube)[o] = y;
-                        else reinterpret_cast<float*>(A.cube)[o] = y.x;
-                    }
+                    store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, y);
                     if constexpr (EPI) {
                         eS.x += y.x;
                         eS.y += y.y;
@@ -591,13 +751,29 @@ __global__ void __launch_bounds__(kTile, 2) das_fast_kernel(const Params A) {
             }
         }
     }
+    cp_async_commit();
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+template <int MODE, bool CPLX, int ST, bool EPI>
+size_t smem_bytes(int64_t N, int64_t W) {
+    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
+    constexpr int NS = ORDER_A ? 2 * 16 : 8 * 4;
+    const size_t entries = (size_t)NS * kSlot * (CPLX ? 16 : 8);
+    const size_t raw = 2 * (size_t)NS * kRawSamples * StoreInfo<ST, CPLX>::bytes;
+    const size_t hdr = 8 * (size_t)(N + W) + (size_t)(N + W);
+    return entries + raw + ((hdr + 15) & ~size_t(15));
 }
 
 template <int MODE, bool CPLX, int ST, bool EPI>
 int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
-    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
-    constexpr int NS = (ORDER_A ? 2 * 16 : 8 * 4);
-    const size_t smem = (size_t)NS * kSlot * (CPLX ? 16 : 8);
+    const size_t smem = smem_bytes<MODE, CPLX, ST, EPI>(A.N, A.W);
+    int dev = 0, optin = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE,
+                 "%lld channels / %lld waves need %zu bytes of shared memory per tile (limit %d)",
+                 (long long)A.N, (long long)A.W, smem, optin);
     auto kern = das_fast_kernel<MODE, CPLX, ST, EPI>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)n_tiles, (unsigned)F);

@@ -1,0 +1,123 @@
+"""Post-DAS steps that follow the fused coherence-factor / simplified-DMAS epilogue.
+
+``simplified_dmas_image`` completes +postprocess/simplified_delay_multiply_and_sum.m
+on a linear scan: the per-pixel value ((sum sign(s) sqrt|s|)^2 - sum |s|)/2
+comes from the fused epilogue of ``ustb_das_fast`` (dimension.transmit); here it is
+band-pass filtered along depth around 2*f0 with the reference's Kaiser design
+(:151-176) on the GPU (``ustb_fir_depth``) and made analytic along depth (:192).
+
+The filter design restates MATLAB's ``kaiserord`` (Kaiser's order and beta
+formulas) followed by ``fir1(n, Wn, kaiser(n+1, beta), 'noscale')``, which is
+scipy's ``firwin(..., scale=False)`` with the same window.  ``estimate_frequency``
+restates +tools/estimate_frequency.m / +tools/power_spectrum.m.
+"""
+from __future__ import annotations
+
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def kaiser_order(f_edges: Sequence[float], devs: Sequence[float], fs: float):
+    """(n, Wn, beta) of MATLAB kaiserord(f, [0 1 0], devs, fs) for a band-pass."""
+    f = np.asarray(f_edges, np.float64) / fs
+    A = -20.0 * math.log10(min(devs))
+    if A > 50:
+        beta = 0.1102 * (A - 8.7)
+    elif A > 21:
+        beta = 0.5842 * (A - 21) ** 0.4 + 0.07886 * (A - 21)
+    else:
+        beta = 0.0
+    df = min(f[1] - f[0], f[3] - f[2])
+    n = int(math.ceil((A - 7.95) / (2 * math.pi * 2.285 * df))) if A > 21 else int(math.ceil(5.79 / (2 * math.pi * df)))
+    Wn = np.array([(f[0] + f[1]), (f[2] + f[3])])  # midpoints, relative to Nyquist
+    return n, Wn, beta
+
+
+def bandpass_taps(f_edges, fs, devs=(1e-3, 1e-3, 1e-3)) -> np.ndarray:
+    from scipy.signal import firwin
+
+    n, Wn, beta = kaiser_order(f_edges, devs, fs)
+    return firwin(n + 1, Wn, window=("kaiser", beta), pass_zero=False, scale=False)
+
+
+def estimate_frequency(time: np.ndarray, data: np.ndarray):
+    """(fc, bw) from the averaged power spectrum along axis 0 (estimate_frequency.m)."""
+    fs = 1.0 / np.mean(np.diff(time))
+    d = data.reshape(data.shape[0], -1)
+    pw = np.fft.fftshift(np.fft.fft(d, axis=0), axes=0)
+    pw = np.mean(np.abs(pw) ** 2, axis=1)
+    pw = pw / pw.max()
+    fx = np.linspace(-fs / 2, fs / 2, data.shape[0] + 1)[:-1]
+    k = np.ones(26) / 26
+    fpw = np.convolve(pw, k)[: pw.size]  # filter(ones(1,26)/26, 1, pw)
+    fpw = np.concatenate([fpw[12:], np.zeros(12)])
+    w = fpw * (fx > 0)
+    ic = int(np.argmax(w))
+    dc = w[ic]
+    fc = fx[ic]
+    up = fx[(fx > fc) & (fpw < dc / 2)]
+    do = fx[(fx < fc) & (fpw < dc / 2)]
+    bw_up = up.min() if up.size else fx[-1]
+    bw_do = do.max() if do.size else 0.0
+    fc = (bw_up + bw_do) / 2
+    return fc, 2 * (bw_up - fc)
+
+
+def fir_depth(x: torch.Tensor, taps: np.ndarray, delay: Optional[int] = None) -> torch.Tensor:
+    """Filter columns of a real (ncols, nz) CUDA tensor along depth with delay compensation."""
+    if x.dtype != torch.float32 or not x.is_cuda:
+        raise TypeError("x must be a float32 CUDA tensor")
+    x = x.contiguous()
+    nz = x.shape[-1]
+    ncols = x.numel() // max(nz, 1)
+    t = torch.as_tensor(np.asarray(taps, np.float32), device=x.device)
+    if delay is None:
+        delay = int(round((t.numel() - 1) / 2))
+    out = torch.empty_like(x)
+    with torch.cuda.device(x.device):
+        _lib.call("ustb_fir_depth", x.data_ptr(), out.data_ptr(), nz, ncols, t.data_ptr(), t.numel(),
+                  delay, torch.cuda.current_stream(x.device).cuda_stream)
+    return out
+
+
+def hilbert_depth(x: torch.Tensor) -> torch.Tensor:
+    """Analytic signal along the last (depth) dimension."""
+    from .das import hilbert_last
+
+    return hilbert_last(x)
+
+
+def simplified_dmas_image(sdmas: torch.Tensor, nz: int, nx: int, z_step: float, sound_speed: float,
+                          f0: Optional[float] = None, filter_freqs=None,
+                          reference_image: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Band-pass + Hilbert of the fused sDMAS value on a linear scan.
+
+    ``sdmas``: (F, P) float32 from ``ustb_das_fast`` (P = nz * nx, depth fastest).
+    The pass band is [1.5 f0, 2.5 f0] with f0/4 transitions unless
+    ``filter_freqs`` gives the four edges.  Without f0 it is estimated from the
+    real part of ``reference_image`` (the channel sum) along depth.  Returns
+    complex64 (F, P).
+    """
+    fs = sound_speed / z_step / 2
+    if filter_freqs is None:
+        if f0 is None:
+            if reference_image is None:
+                raise ValueError("give f0, filter_freqs or a reference image")
+            img = reference_image.real.reshape(-1, nx, nz).permute(2, 1, 0).cpu().numpy()
+            t = 2 * np.arange(nz) * z_step / sound_speed
+            f0, _ = estimate_frequency(t, img)
+        F_edges = [1.5 * f0, 1.5 * f0 + f0 / 4, 2.5 * f0, 2.5 * f0 + f0 / 4]
+    else:
+        F_edges = list(filter_freqs)
+    if not fs / 2 > F_edges[-1]:
+        raise ValueError(f"need {math.ceil(F_edges[-1] * 2 / fs)} times more depth samples for the "
+                         "DMAS band-pass around 2*f0")
+    taps = bandpass_taps(F_edges, fs)
+    y = sdmas.reshape(-1, nx, nz).to(torch.float32)
+    filt = fir_depth(y.reshape(-1, nz), taps).reshape(-1, nx, nz)
+    return hilbert_depth(filt).reshape(sdmas.shape[0], -1)
