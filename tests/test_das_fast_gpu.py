@@ -274,8 +274,8 @@ def test_sdmas_bandpass_and_hilbert_follow_up(cuda_dev):
 def test_kaiser_design_matches_kaiser_formulas():
     from ustb_gb300.postprocess import bandpass_taps, kaiser_order
 
-    n, Wn, beta = kaiser_order([7.5e6, 8.75e6, 12.5e6, 13.75e6], [1e-3] * 3, 1540 / 0.05e-3 / 2)
+    n, Wn, beta = kaiser_order([7.5e6, 8.75e6, 12.5e6, 13.75e6], [1e-3] * 3, 1540 / 0.02e-3 / 2)
     assert beta == pytest.approx(0.1102 * (60 - 8.7))
-    assert n == math.ceil((60 - 7.95) / (2 * math.pi * 2.285 * (1.25e6 / (1540 / 0.05e-3 / 2))))
-    taps = bandpass_taps([7.5e6, 8.75e6, 12.5e6, 13.75e6], 1540 / 0.05e-3 / 2)
+    assert n == math.ceil((60 - 7.95) / (2 * math.pi * 2.285 * (1.25e6 / (1540 / 0.02e-3 / 2))))
+    taps = bandpass_taps([7.5e6, 8.75e6, 12.5e6, 13.75e6], 1540 / 0.02e-3 / 2)
     assert taps.size == n + 1 and np.allclose(taps, taps[::-1])
