@@ -167,7 +167,7 @@ enum {
 };
 
 /* Pixels per tile of the fast path (one CTA). */
-#define USTB_TILE_PIXELS 256
+#define USTB_TILE_PIXELS 512
 
 /*
  * Geometry of one beamforming request.  All pointers are device pointers.

@@ -204,13 +204,18 @@ def test_window_overflow_is_flagged_not_faulted(cuda_dev):
     probe, scan, seq, fs, f0, ch = linear_setup(rng, W=2)
     # one tile spanning the whole scan: far too long a window
     P = scan.N_pixels
-    tiles = np.full(((P + 255) // 256, 256), -1, np.int32)
+    T = fast.TILE
+    tiles = np.full(((P + T - 1) // T, T), -1, np.int32)
     order = np.random.default_rng(0).permutation(P)
     tiles.ravel()[:P] = order
     g = fast.FastGeometry(probe, scan, seq, fs, 1e-6, f0, 1540.0, cuda_dev, Apodization(), None, tiles=tiles)
     with pytest.raises(_lib.UstbError) as e:
         run_fast(ch, Precision.fp16, g, 3)
     assert e.value.code == 7
+    # malformed tile maps are refused on the host
+    with pytest.raises(ValueError):
+        fast.FastGeometry(probe, scan, seq, fs, 1e-6, f0, 1540.0, cuda_dev, Apodization(), None,
+                          tiles=np.zeros((1, 256), np.int32))
     # the device is still healthy afterwards
     g_ok = fast.FastGeometry(probe, scan, seq, fs, 1e-6, f0, 1540.0, cuda_dev, Apodization(), None)
     run_fast(ch, Precision.fp16, g_ok, 3)

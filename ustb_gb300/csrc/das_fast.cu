@@ -8,7 +8,7 @@
 //   y = sum_w sum_n  A_w(p) * B_n(p) * lerp(x_{n,w}, s_tx(p,w) + s_rx(p,n))
 //   A_w = apo_tx * exp(i 2 pi fd tau_tx),  B_n = apo_rx * exp(i 2 pi fd tau_rx)
 //
-// One CTA beamforms a tile of 256 pixels (one per thread) for one frame.  The
+// One CTA beamforms a tile of 512 pixels (one per thread) for one frame.  The
 // (channel, wave) pairs are processed in stages of CG x KW; for each pair the
 // tile needs a short window of samples starting at i0 = base_n + base_w, where
 // base_n / base_w are integer lower bounds of the tile's receive / transmit
@@ -17,7 +17,7 @@
 // validity rule (0 < i < L-1) folded in as zero entries, so a unit costs:
 //   s = s_tx_loc + s_rx_loc; j = floor(s); b = s - j; e = slot[j];
 //   v = e.x + b*e.d;  acc += weight * v.
-// Delays relative to the tile bases stay below 64 samples, so j and b keep
+// Delays relative to the tile bases stay below 80 samples, so j and b keep
 // full sub-sample precision in FP32.
 //
 // Loop orders: waves outer / channels inner for dimension.both and .receive
@@ -32,7 +32,7 @@
 namespace {
 
 constexpr int kTile = USTB_TILE_PIXELS;
-constexpr int kSlot = 128;                      // entries per (channel, wave) window
+constexpr int kSlot = 160;                      // entries per (channel, wave) window
 constexpr float kHalf = (float)(kSlot / 2 - 1);  // max relative delay of each component
 constexpr float kMagic = 8388608.0f;            // 2^23: floor via round-toward-zero add
 constexpr int kMagicBits = 0x4B000000;
@@ -61,49 +61,6 @@ struct Params {
     float* o_sdmas;
     int64_t rx_f, w_f, f_f;
     uint32_t* flags;
-};
-
-// ---------------------------------------------------------------------------
-// sample loads
-// ---------------------------------------------------------------------------
-template <int ST, bool CPLX>
-struct Sample;
-
-template <>
-struct Sample<USTB_STORE_F32, true> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return __ldg(reinterpret_cast<const float2*>(base) + i);
-    }
-};
-template <>
-struct Sample<USTB_STORE_F16, true> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return __half22float2(__ldg(reinterpret_cast<const __half2*>(base) + i));
-    }
-};
-template <>
-struct Sample<USTB_STORE_BF16, true> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(base) + i));
-    }
-};
-template <>
-struct Sample<USTB_STORE_F32, false> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return make_float2(__ldg(reinterpret_cast<const float*>(base) + i), 0.f);
-    }
-};
-template <>
-struct Sample<USTB_STORE_F16, false> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return make_float2(__half2float(__ldg(reinterpret_cast<const __half*>(base) + i)), 0.f);
-    }
-};
-template <>
-struct Sample<USTB_STORE_BF16, false> {
-    static __device__ __forceinline__ float2 load(const void* base, int64_t i) {
-        return make_float2(__bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(base) + i)), 0.f);
-    }
 };
 
 // ---------------------------------------------------------------------------
@@ -157,10 +114,12 @@ __device__ __forceinline__ float rx_apodization(const Params& A, float ex, float
         zd = pz - ez;
     }
     const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
-    const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
     const float rt = fabsf(A.fnx * __fdividef(xd, zx));
+    const float wx = window(A.rx_window, rt);
+    if (yd == 0.f) return wx * window(A.rx_window, 0.f);  // 1-D arrays: elevation ratio 0
+    const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
     const float rp = fabsf(A.fny * __fdividef(yd, zy));
-    return window(A.rx_window, rt) * window(A.rx_window, rp);
+    return wx * window(A.rx_window, rp);
 }
 
 // exp(i 2 pi fd tau) from the phase in cycles
@@ -196,14 +155,14 @@ __device__ __forceinline__ float tx_tau(const Params& A, const ustb_wave& wv, in
                                         float px, float py, float pz) {
     switch (wv.kind) {
         case USTB_WAVE_PLANE:
-            return (px * wv.dir[0] + py * wv.dir[1] + pz * wv.dir[2]) / wv.sound_speed - wv.delay;
+            return __fdividef(px * wv.dir[0] + py * wv.dir[1] + pz * wv.dir[2], wv.sound_speed) - wv.delay;
         case USTB_WAVE_SPHERICAL: {
             const float dx = px - wv.src[0], dy = py - wv.src[1], dz = pz - wv.src[2];
             const float d = sqrtf(dx * dx + dy * dy + dz * dz);
             const float sg = pz < wv.src[2] ? -1.f : 1.f;
-            return (sg * d + wv.offset) / wv.sound_speed - wv.delay;
+            return __fdividef(sg * d + wv.offset, wv.sound_speed) - wv.delay;
         }
-        case USTB_WAVE_TABLE: return __ldg(A.tx_delay_tab + w * A.P + p);
+        case USTB_WAVE_TABLE: return A.tx_delay_tab ? __ldg(A.tx_delay_tab + w * A.P + p) : -wv.delay;
         default: return -wv.delay;
     }
 }
@@ -324,7 +283,7 @@ __device__ __forceinline__ bool rx_active(const Params& A, const Box& b, float e
 
 template <bool CPLX, int ST>
 struct CtasPerSm {
-    static constexpr int value = (CPLX && ST == USTB_STORE_F32) ? 1 : 2;
+    static constexpr int value = 1;  // 512 threads x 128 registers fill the register file
 };
 
 template <int MODE, bool CPLX, int ST, bool EPI>
@@ -344,21 +303,28 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
     extern __shared__ __align__(16) unsigned char smem[];
     Entry* slots = reinterpret_cast<Entry*>(smem);
     unsigned char* raw_base = smem + (size_t)NS * kSlot * sizeof(Entry);
-    int* base_n = reinterpret_cast<int*>(raw_base + 2 * NS * RAWB);
-    int* len_n = base_n + N;
-    int* base_w = len_n + N;
-    int* len_w = base_w + W;
-    unsigned char* act_n = reinterpret_cast<unsigned char*>(len_w + W);
+    const int NG = (int)((N + CG - 1) / CG), NC = (int)((W + KW - 1) / KW);
+    float* base_n = reinterpret_cast<float*>(raw_base + 2 * NS * RAWB);  // integer-valued
+    int* len_n = reinterpret_cast<int*>(base_n + N);
+    float* base_w = reinterpret_cast<float*>(len_n + N);
+    int* len_w = reinterpret_cast<int*>(base_w + W);
+    int* stage_list = len_w + W;  // (outer index << 16) | inner index, loop order
+    unsigned char* act_n = reinterpret_cast<unsigned char*>(stage_list + NG * NC);
     unsigned char* act_w = act_n + N;
+    unsigned char* act_g = act_w + W;  // channel groups
+    unsigned char* act_c = act_g + NG; // wave chunks
     __shared__ float2 s_red[kTile / 32];
+    __shared__ int s_nstages;
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int64_t f = blockIdx.y;
     const int32_t* tl = A.tiles + (int64_t)blockIdx.x * kTile;
+    // tile entries outside [0, P) are idle lanes; lane 0 names the tile's anchor pixel
     const int32_t p_own = __ldg(tl + tid);
-    const bool live = p_own >= 0;
-    const int64_t p = live ? p_own : __ldg(tl);
+    const bool live = p_own >= 0 && (int64_t)p_own < A.P;
+    const int32_t p_anchor = __ldg(tl);
+    const int64_t p = live ? p_own : ((p_anchor >= 0 && (int64_t)p_anchor < A.P) ? p_anchor : 0);
     const float px = __ldg(A.px + 3 * p), py = __ldg(A.px + 3 * p + 1), pz = __ldg(A.px + 3 * p + 2);
 
     Box box;
@@ -382,7 +348,7 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
         const bool ok = (hi - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
         const bool act = rx_active(A, box, ex, ey, ez);
         if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-        base_n[n] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        base_n[n] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
         len_n[n] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
         act_n[n] = act ? 1 : 0;
     }
@@ -397,7 +363,7 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
         const bool ok = (hi - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
         const bool act = A.tx_apo_tab != nullptr || wv.apodization != 0.f;
         if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-        base_w[w] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        base_w[w] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
         len_w[w] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
         act_w[w] = act ? 1 : 0;
     }
@@ -410,13 +376,37 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
                 const float base = floorf(r.x) - 1.f;
                 const bool ok = (r.y - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
                 if (!ok) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-                base_w[w] = (int)fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                base_w[w] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
                 len_w[w] = (int)fminf(fmaxf(ceilf(r.y - base), 0.f), kHalf);
                 act_w[w] = 1;
             }
         }
     }
     __syncthreads();
+    for (int g = tid; g < NG; g += kTile) {
+        bool a = false;
+        for (int c = 0; c < CG; ++c) a |= (g * CG + c < N) && act_n[g * CG + c];
+        act_g[g] = a;
+    }
+    for (int k = tid; k < NC; k += kTile) {
+        bool a = false;
+        for (int j = 0; j < KW; ++j) a |= (k * KW + j < W) && act_w[k * KW + j];
+        act_c[k] = a;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int cnt = 0;
+        const int NO = ORDER_A ? NC : NG, NI = ORDER_A ? NG : NC;
+        const unsigned char* ao = ORDER_A ? act_c : act_g;
+        const unsigned char* ai = ORDER_A ? act_g : act_c;
+        for (int o = 0; o < NO; ++o)
+            if (ao[o])
+                for (int i = 0; i < NI; ++i)
+                    if (ai[i]) stage_list[cnt++] = (o << 16) | i;
+        s_nstages = cnt;
+    }
+    __syncthreads();
+    const int nstages = s_nstages;
 
     const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
     const float fd_c = A.fd * A.inv_c;
@@ -424,46 +414,53 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
     const int64_t TOT = L * N * W * A.F;  // samples in the whole array
     const int64_t frame_off = f * W * N * L;
 
-    auto group_active = [&](int64_t n0) {
-        bool a = false;
-#pragma unroll
-        for (int c = 0; c < CG; ++c) a |= (n0 + c < N) && act_n[n0 + c];
-        return a;
+    // Per-slot staging metadata.  Each warp owns SPW slots of every stage
+    // (slot = warp + NWARPS * r); lane r computes slot r's metadata once and the
+    // warp reads it back with shuffles.
+    constexpr int NWARPS = kTile / 32;
+    constexpr int SPW = (NS + NWARPS - 1) / NWARPS;
+    static_assert(SPW <= 32, "too many slots per warp");
+    struct Meta {
+        int64_t tb;  // global sample index of the trace start
+        int i0, len, act;
     };
-    auto chunk_active = [&](int64_t w0) {
-        bool a = false;
-#pragma unroll
-        for (int k = 0; k < KW; ++k) a |= (w0 + k < W) && act_w[w0 + k];
-        return a;
-    };
-    // next active stage after (o, i) in loop order: outer index o, inner i
-    const int64_t OUTS = ORDER_A ? KW : CG, INS = ORDER_A ? CG : KW;
-    const int64_t OUTN = ORDER_A ? W : N, INN = ORDER_A ? N : W;
-    auto stage_active = [&](int64_t o, int64_t i) {
-        return ORDER_A ? (chunk_active(o) && group_active(i)) : (group_active(o) && chunk_active(i));
-    };
-    auto advance = [&](int64_t& o, int64_t& i) -> bool {
-        for (;;) {
-            i += INS;
-            if (i >= INN) { i = 0; o += OUTS; }
-            if (o >= OUTN) return false;
-            if (stage_active(o, i)) return true;
+    auto meta_of = [&](int w0, int n0) {
+        Meta m{0, 0, 0, 0};
+        const int slot = warp + NWARPS * lane;
+        if (lane < SPW && slot < NS) {
+            const int c = slot / KW, k = slot - c * KW;
+            const int n = n0 + c, w = w0 + k;
+            if (n < N && w < W && act_n[n] && act_w[w]) {
+                m.act = 1;
+                m.len = min(kSlot, len_n[n] + len_w[w] + 3);
+                m.i0 = __float2int_rn(base_n[n] + base_w[w]);
+                m.tb = frame_off + ((int64_t)w * N + n) * L;
+            }
         }
+        return m;
+    };
+    auto bcast = [&](const Meta& m, int r) {
+        Meta o;
+        o.tb = __shfl_sync(0xffffffffu, m.tb, r);
+        o.i0 = __shfl_sync(0xffffffffu, m.i0, r);
+        o.len = __shfl_sync(0xffffffffu, m.len, r);
+        o.act = __shfl_sync(0xffffffffu, m.act, r);
+        return o;
     };
 
-    // issue the raw copies of stage (w0, n0) into buffer b
-    auto issue = [&](int64_t w0, int64_t n0, int b) {
+    // issue the raw copies of the stage described by `m` into buffer b
+    auto issue = [&](const Meta& m, int b) {
         unsigned char* rb = raw_base + b * NS * RAWB;
-        for (int slot = warp; slot < NS; slot += kTile / 32) {
-            const int c = slot / KW, k = slot - c * KW;
-            const int64_t n = n0 + c, w = w0 + k;
-            if (n >= N || w >= W || !act_n[n] || !act_w[w]) continue;
-            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
-            const int64_t g0 = frame_off + (w * N + n) * L + base_n[n] + base_w[w];
-            const int64_t ga = g0 >= 0 ? (g0 / SPC) * SPC : -(((-g0) + SPC - 1) / SPC) * SPC;
-            const int nch = (int)((g0 - ga + len + 1 + SPC - 1) / SPC);
+#pragma unroll
+        for (int r = 0; r < SPW; ++r) {
+            const int slot = warp + NWARPS * r;
+            const Meta q = bcast(m, r);
+            if (slot >= NS || !q.act) continue;
+            const int64_t g0 = q.tb + q.i0;
+            const int64_t ga = g0 & ~(int64_t)(SPC - 1);
+            const int nch = ((int)(g0 - ga) + q.len + 1 + SPC - 1) / SPC;
             unsigned char* dst = rb + slot * RAWB;
-            for (int ch = lane; ch < nch && ch < MAXCH; ch += 32) {
+            for (int ch = lane; ch < nch; ch += 32) {
                 const int64_t cs = ga + (int64_t)ch * SPC;
                 if (cs >= 0 && cs + SPC <= TOT) {
                     cp_async16(dst + ch * 16, chb + cs * SB);
@@ -481,34 +478,32 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
         cp_async_commit();
     };
 
-    // raw samples -> interpolation entries {x_i, x_{i+1} - x_i} with das_c's validity rule
-    auto transform = [&](int64_t w0, int64_t n0, int b) {
+    // raw samples -> interpolation entries {x_i, x_{i+1} - x_i} with das_c's
+    // validity rule (0 < i < L-1); slots without work get zero entries
+    const unsigned Lm2 = (unsigned)(L - 2);
+    auto transform = [&](const Meta& m, int b) {
         const unsigned char* rb = raw_base + b * NS * RAWB;
-        for (int slot = warp; slot < NS; slot += kTile / 32) {
-            const int c = slot / KW, k = slot - c * KW;
-            const int64_t n = n0 + c, w = w0 + k;
-            if (n >= N || w >= W || !act_n[n] || !act_w[w]) {
-                // units of this slot carry zero weight and read j <= kHalf: make those zeros
-                Entry* dz = slots + slot * kSlot;
+#pragma unroll
+        for (int r = 0; r < SPW; ++r) {
+            const int slot = warp + NWARPS * r;
+            if (slot >= NS) continue;
+            const Meta q = bcast(m, r);
+            Entry* dst = slots + slot * kSlot;
+            if (!q.act) {
+                // units of this slot carry zero weight and read j <= kHalf
                 for (int j = lane; j <= (int)kHalf; j += 32) {
-                    if constexpr (CPLX) dz[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    else dz[j] = make_float2(0.f, 0.f);
+                    if constexpr (CPLX) dst[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    else dst[j] = make_float2(0.f, 0.f);
                 }
                 continue;
             }
-            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
-            const int64_t i0 = (int64_t)base_n[n] + base_w[w];
-            const int64_t g0 = frame_off + (w * N + n) * L + i0;
-            const int64_t ga = g0 >= 0 ? (g0 / SPC) * SPC : -(((-g0) + SPC - 1) / SPC) * SPC;
-            const int off = (int)(g0 - ga);
+            const int off = (int)((q.tb + q.i0) & (int64_t)(SPC - 1));
             const unsigned char* src = rb + slot * RAWB;
-            Entry* dst = slots + slot * kSlot;
-            for (int j = lane; j < len; j += 32) {
-                const int64_t i = i0 + j;
+            for (int j = lane; j < q.len; j += 32) {
                 Entry v;
                 if constexpr (CPLX) v = make_float4(0.f, 0.f, 0.f, 0.f);
                 else v = make_float2(0.f, 0.f);
-                if (i >= 1 && i <= L - 2) {
+                if ((unsigned)(q.i0 + j - 1) < Lm2) {
                     const float2 x0 = raw_sample<ST, CPLX>(src, off + j);
                     const float2 x1 = raw_sample<ST, CPLX>(src, off + j + 1);
                     if constexpr (CPLX) v = make_float4(x0.x, x0.y, x1.x - x0.x, x1.y - x0.y);
@@ -531,10 +526,10 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
     float2 eS = make_float2(0.f, 0.f);
     float eI = 0.f, eM = 0.f, eR = 0.f, eQ = 0.f;
 
-    auto setup_rx = [&](int64_t n0) {
+    auto setup_rx = [&](int n0) {
 #pragma unroll
         for (int c = 0; c < CG; ++c) {
-            const int64_t n = n0 + c;
+            const int n = n0 + c;
             float s = 0.f, apo = 0.f;
             float2 bb = make_float2(0.f, 0.f);
             if (n < N && act_n[n]) {
@@ -542,8 +537,8 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
                 const float dx = px - ex, dy = py - ey, dz = pz - ez;
                 const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-30f);
                 const float r = r2 * rsqrtf(r2);
-                s = (r * A.inv_c + A.lens) * A.fs - (float)base_n[n];
-                apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
+                s = (r * A.inv_c + A.lens) * A.fs - base_n[n];
+                apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + (int64_t)n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
                 if (!live) apo = 0.f;
                 if (CPLX) {
                     const float2 e = phasor_cycles(r * fd_c + A.lens * A.fd);
@@ -557,17 +552,17 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
             rxapo[c] = apo;
         }
     };
-    auto setup_tx = [&](int64_t w0) {
+    auto setup_tx = [&](int w0) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) {
-            const int64_t w = w0 + k;
+            const int w = w0 + k;
             float s = 0.f, apo = 0.f;
             float2 a = make_float2(0.f, 0.f);
             if (w < W && act_w[w]) {
                 const ustb_wave wv = A.waves[w];
                 const float tau = tx_tau(A, wv, w, p, px, py, pz);
-                s = (tau - A.t0) * A.fs - (float)base_w[w];
-                apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + w * P + p) : wv.apodization;
+                s = (tau - A.t0) * A.fs - base_w[w];
+                apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + (int64_t)w * P + p) : wv.apodization;
                 if (!live) apo = 0.f;
                 if (CPLX) {
                     const float2 e = phasor_cycles(tau * A.fd);
@@ -606,56 +601,43 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
         else reinterpret_cast<float*>(A.cube)[o] = y.x;
     };
 
-    // first active stage
-    int64_t no = 0, ni = -INS;
-    bool have_next = advance(no, ni);
+    // pipeline over the tile's active stages: stage si+1's copies are in flight
+    // while stage si is transformed and computed
     int buf = 0;
-    if (have_next) issue(ORDER_A ? no : ni, ORDER_A ? ni : no, buf);
-
-    // one pipelined stage: copies for the next stage go out before this one is used
-    auto run_stage = [&](int64_t w0, int64_t n0) {
-        int64_t o2 = no, i2 = ni;
-        const bool more = advance(o2, i2);
-        if (more) issue(ORDER_A ? o2 : i2, ORDER_A ? i2 : o2, buf ^ 1);
-        else cp_async_commit();  // keep one group per stage
-        no = o2; ni = i2;
+    auto stage_o = [&](int si) { return stage_list[si] >> 16; };
+    auto stage_i = [&](int si) { return stage_list[si] & 0xFFFF; };
+    auto stage_w0 = [&](int si) { return (ORDER_A ? stage_o(si) : stage_i(si)) * KW; };
+    auto stage_n0 = [&](int si) { return (ORDER_A ? stage_i(si) : stage_o(si)) * CG; };
+    Meta m_cur{0, 0, 0, 0}, m_nxt{0, 0, 0, 0};
+    if (nstages > 0) {
+        m_cur = meta_of(stage_w0(0), stage_n0(0));
+        issue(m_cur, 0);
+    }
+    auto run_stage = [&](int si) {
+        if (si + 1 < nstages) {
+            m_nxt = meta_of(stage_w0(si + 1), stage_n0(si + 1));
+            issue(m_nxt, buf ^ 1);
+        } else {
+            cp_async_commit();  // keep one group per stage
+        }
         cp_async_wait_prev();
-        __syncthreads();  // raw(s) visible everywhere; previous stage's entries consumed
-        transform(w0, n0, buf);
+        __syncthreads();  // raw(si) visible everywhere; previous stage's entries consumed
+        transform(m_cur, buf);
         __syncthreads();
+        m_cur = m_nxt;
         buf ^= 1;
     };
+    const float2 zero2 = make_float2(0.f, 0.f);
 
     if constexpr (ORDER_A) {
-        for (int64_t w0 = 0; w0 < W; w0 += KW) {
-            const int kw = (int)min((int64_t)KW, W - w0);
-            if (!chunk_active(w0)) {
-                if (MODE == USTB_DIM_RECEIVE)
-                    for (int k = 0; k < kw; ++k) store_cube(p + A.w_f * (w0 + k) + A.f_f * f, make_float2(0.f, 0.f));
-                continue;
-            }
-            setup_tx(w0);
-#pragma unroll
-            for (int k = 0; k < KW; ++k) accr[k] = acci[k] = 0.f;
-            for (int64_t n0 = 0; n0 < N; n0 += CG) {
-                if (!group_active(n0)) continue;
-                run_stage(w0, n0);
-                setup_rx(n0);
-#pragma unroll
-                for (int c = 0; c < CG; ++c) {
-                    const float2 b = B[c];
-#pragma unroll
-                    for (int k = 0; k < KW; ++k) {
-                        const float2 v = interp(c, k, stx[k] + srx[c]);
-                        if constexpr (CPLX) {
-                            accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
-                            acci[k] = fmaf(b.x, v.y, fmaf(b.y, v.x, acci[k]));
-                        } else {
-                            accr[k] = fmaf(b.x, v.x, accr[k]);
-                        }
-                    }
-                }
-            }
+        int cur = -1;  // current wave chunk
+        auto zero_chunks = [&](int from, int to) {  // receive mode: skipped chunks are zero
+            if (MODE != USTB_DIM_RECEIVE) return;
+            for (int w = from * KW; w < min(to * KW, (int)W); ++w) store_cube(p + A.w_f * w + A.f_f * f, zero2);
+        };
+        auto finish_chunk = [&]() {
+            const int w0 = cur * KW;
+            const int kw = min(KW, (int)W - w0);
 #pragma unroll
             for (int k = 0; k < KW; ++k) {
                 if (k >= kw) continue;
@@ -669,76 +651,105 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
                     store_cube(p + A.w_f * (w0 + k) + A.f_f * f, CPLX ? cmul(y, ph) : y);
                 }
             }
-        }
-        if (MODE == USTB_DIM_BOTH) store_cube(p + A.f_f * f, CPLX ? cmul(Y, ph) : Y);
-    } else {
-        for (int64_t n0 = 0; n0 < N; n0 += CG) {
-            const int cg = (int)min((int64_t)CG, N - n0);
-            if (!group_active(n0)) {
-                for (int c = 0; c < cg; ++c) {
-                    if (MODE == USTB_DIM_TRANSMIT) store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, make_float2(0.f, 0.f));
-                    if (MODE == USTB_DIM_NONE)
-                        for (int64_t w = 0; w < W; ++w)
-                            store_cube(p + A.rx_f * (n0 + c) + A.w_f * w + A.f_f * f, make_float2(0.f, 0.f));
-                }
-                continue;
+        };
+        for (int si = 0; si < nstages; ++si) {
+            const int oc = stage_o(si);
+            if (oc != cur) {
+                if (cur >= 0) finish_chunk();
+                zero_chunks(cur + 1, oc);
+                cur = oc;
+                setup_tx(oc * KW);
+#pragma unroll
+                for (int k = 0; k < KW; ++k) accr[k] = acci[k] = 0.f;
             }
+            const int n0 = stage_n0(si);
+            run_stage(si);
             setup_rx(n0);
 #pragma unroll
-            for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
-            for (int64_t w0 = 0; w0 < W; w0 += KW) {
-                const int kw = (int)min((int64_t)KW, W - w0);
-                const bool ca = chunk_active(w0);
-                if (ca) {
-                    run_stage(w0, n0);
-                    setup_tx(w0);
-                }
+            for (int c = 0; c < CG; ++c) {
+                const float2 b = B[c];
 #pragma unroll
-                for (int c = 0; c < CG; ++c) {
-#pragma unroll
-                    for (int k = 0; k < KW; ++k) {
-                        if (MODE == USTB_DIM_NONE) {
-                            const bool u = ca && (n0 + c < N) && act_n[n0 + c] && (w0 + k < W) && act_w[w0 + k];
-                            if (c < cg && k < kw) {
-                                float2 y = make_float2(0.f, 0.f);
-                                if (u) {
-                                    const float2 v = interp(c, k, stx[k] + srx[c]);
-                                    y = CPLX ? cmul(cmul(cmul(Aw[k], B[c]), v), ph) : make_float2(Aw[k].x * B[c].x * v.x, 0.f);
-                                }
-                                store_cube(p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f, y);
-                            }
-                        } else if (ca) {
-                            const float2 v = interp(c, k, stx[k] + srx[c]);
-                            if constexpr (CPLX) {
-                                accr[c] = fmaf(Aw[k].x, v.x, fmaf(-Aw[k].y, v.y, accr[c]));
-                                acci[c] = fmaf(Aw[k].x, v.y, fmaf(Aw[k].y, v.x, acci[c]));
-                            } else {
-                                accr[c] = fmaf(Aw[k].x, v.x, accr[c]);
-                            }
-                        }
-                    }
-                }
-            }
-            if (MODE == USTB_DIM_TRANSMIT) {
-#pragma unroll
-                for (int c = 0; c < CG; ++c) {
-                    if (c >= cg) continue;
-                    float2 y;
-                    if constexpr (CPLX) y = cmul(cmul(B[c], make_float2(accr[c], acci[c])), ph);
-                    else y = make_float2(B[c].x * accr[c], 0.f);
-                    store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, y);
-                    if constexpr (EPI) {
-                        eS.x += y.x;
-                        eS.y += y.y;
-                        eI += y.x * y.x + y.y * y.y;
-                        eM += rxapo[c] > A.cf_thr ? 1.f : 0.f;
-                        const float re = y.x;
-                        eR += msign(re) * sqrtf(fabsf(re));
-                        eQ += fabsf(re);
+                for (int k = 0; k < KW; ++k) {
+                    const float2 v = interp(c, k, stx[k] + srx[c]);
+                    if constexpr (CPLX) {
+                        accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
+                        acci[k] = fmaf(b.x, v.y, fmaf(b.y, v.x, acci[k]));
+                    } else {
+                        accr[k] = fmaf(b.x, v.x, accr[k]);
                     }
                 }
             }
         }
+        if (cur >= 0) finish_chunk();
+        zero_chunks(cur + 1, NC);
+        if (MODE == USTB_DIM_BOTH) store_cube(p + A.f_f * f, CPLX ? cmul(Y, ph) : Y);
+    } else {
+        if (MODE == USTB_DIM_NONE) {  // units outside the active stages are zero
+            for (int n = 0; n < N; ++n)
+                for (int w = 0; w < W; ++w) store_cube(p + A.rx_f * n + A.w_f * w + A.f_f * f, zero2);
+        }
+        int cur = -1;  // current channel group
+        auto zero_groups = [&](int from, int to) {
+            if (MODE != USTB_DIM_TRANSMIT) return;
+            for (int n = from * CG; n < min(to * CG, (int)N); ++n) store_cube(p + A.rx_f * n + A.f_f * f, zero2);
+        };
+        auto finish_group = [&]() {
+            const int n0 = cur * CG;
+            const int cg = min(CG, (int)N - n0);
+            if (MODE != USTB_DIM_TRANSMIT) return;
+#pragma unroll
+            for (int c = 0; c < CG; ++c) {
+                if (c >= cg) continue;
+                float2 y;
+                if constexpr (CPLX) y = cmul(cmul(B[c], make_float2(accr[c], acci[c])), ph);
+                else y = make_float2(B[c].x * accr[c], 0.f);
+                store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, y);
+                if constexpr (EPI) {
+                    eS.x += y.x;
+                    eS.y += y.y;
+                    eI += y.x * y.x + y.y * y.y;
+                    eM += rxapo[c] > A.cf_thr ? 1.f : 0.f;
+                    const float re = y.x;
+                    eR += msign(re) * sqrtf(fabsf(re));
+                    eQ += fabsf(re);
+                }
+            }
+        };
+        for (int si = 0; si < nstages; ++si) {
+            const int og = stage_o(si);
+            if (og != cur) {
+                if (cur >= 0) finish_group();
+                zero_groups(cur + 1, og);
+                cur = og;
+                setup_rx(og * CG);
+#pragma unroll
+                for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
+            }
+            const int w0 = stage_w0(si), n0 = og * CG;
+            run_stage(si);
+            setup_tx(w0);
+#pragma unroll
+            for (int c = 0; c < CG; ++c) {
+#pragma unroll
+                for (int k = 0; k < KW; ++k) {
+                    const float2 v = interp(c, k, stx[k] + srx[c]);
+                    if (MODE == USTB_DIM_NONE) {
+                        if (n0 + c < N && w0 + k < W && act_n[n0 + c] && act_w[w0 + k]) {
+                            const float2 y = CPLX ? cmul(cmul(cmul(Aw[k], B[c]), v), ph)
+                                                  : make_float2(Aw[k].x * B[c].x * v.x, 0.f);
+                            store_cube(p + A.rx_f * (n0 + c) + A.w_f * (w0 + k) + A.f_f * f, y);
+                        }
+                    } else if constexpr (CPLX) {
+                        accr[c] = fmaf(Aw[k].x, v.x, fmaf(-Aw[k].y, v.y, accr[c]));
+                        acci[c] = fmaf(Aw[k].x, v.y, fmaf(Aw[k].y, v.x, acci[c]));
+                    } else {
+                        accr[c] = fmaf(Aw[k].x, v.x, accr[c]);
+                    }
+                }
+            }
+        }
+        if (cur >= 0) finish_group();
+        zero_groups(cur + 1, NG);
         if constexpr (EPI) {
             if (live) {
                 const int64_t o = p + P * f;
@@ -761,7 +772,9 @@ size_t smem_bytes(int64_t N, int64_t W) {
     constexpr int NS = ORDER_A ? 2 * 16 : 8 * 4;
     const size_t entries = (size_t)NS * kSlot * (CPLX ? 16 : 8);
     const size_t raw = 2 * (size_t)NS * kRawSamples * StoreInfo<ST, CPLX>::bytes;
-    const size_t hdr = 8 * (size_t)(N + W) + (size_t)(N + W);
+    const int CG = ORDER_A ? 2 : 8, KW = ORDER_A ? 16 : 4;
+    const size_t NG = (size_t)((N + CG - 1) / CG), NC = (size_t)((W + KW - 1) / KW);
+    const size_t hdr = 8 * (size_t)(N + W) + 4 * NG * NC + (size_t)(N + W) + NG + NC;
     return entries + raw + ((hdr + 15) & ~size_t(15));
 }
 
@@ -815,6 +828,7 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
                  "the coherence-factor / DMAS epilogue needs dimension.transmit and complex data");
     USTB_REQUIRE(flags, USTB_E_ARG, "flags pointer is NULL");
     USTB_REQUIRE(F <= 65535, USTB_E_SHAPE, "at most 65535 frames per call");
+    USTB_REQUIRE(L <= INT32_MAX - 256, USTB_E_SHAPE, "L=%lld exceeds the 32-bit sample index", (long long)L);
     USTB_REQUIRE(g->n_tiles <= INT32_MAX, USTB_E_SHAPE, "too many tiles");
     USTB_REQUIRE(g->sound_speed > 0.f && g->fs > 0.f, USTB_E_ARG, "sound speed and fs must be > 0");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -823,6 +837,7 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     USTB_REQUIRE(g->element_xyz && g->pixel_xyz && g->tile_pixels && (W == 0 || g->waves), USTB_E_ARG,
                  "a geometry pointer is NULL");
     USTB_REQUIRE(L == 0 || N == 0 || W == 0 || ch, USTB_E_ARG, "channel data pointer is NULL");
+    USTB_REQUIRE(((uintptr_t)ch & 15) == 0, USTB_E_ARG, "channel data must be 16-byte aligned");
     const int64_t P = g->n_pixels;
     if (L == 0 || N == 0 || W == 0) {
         const int64_t nout = out_elems(dimension, P, N, W, F);

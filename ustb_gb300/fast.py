@@ -3,7 +3,7 @@
 ``FastGeometry`` turns a probe / scan / sequence / apodization description
 (the inputs of midprocess.das) into the device-side ``ustb_das_geometry`` of
 the C-ABI: element and pixel positions, one ``ustb_wave`` per transmit event,
-and a tile map that groups pixels into compact tiles of 256 so that every
+and a tile map that groups pixels into compact tiles of 512 so that every
 (channel, wave) sample window of a tile stays short (``plan_tiles``).  Anything
 the kernel cannot form on the fly (focused waves in the hybrid margin, the
 unified and blended models, tilted or vector apodizations) is passed as a
@@ -23,9 +23,9 @@ from .enums import Dimension, Precision, SphericalTransmitDelayModel as STDM, Wa
 from .geometry import Apodization
 from .uff import LinearScan, Probe, Scan, SectorScan, Wave
 
-TILE = 256
-SLOT_HALF = 63          # kernel: max relative delay (samples) of each component
-SPAN_LIMIT = 58.0       # planner: keep tile spans below this many samples
+TILE = 512
+SLOT_HALF = 79          # kernel: max relative delay (samples) of each component
+SPAN_LIMIT = 74.0       # planner: keep tile spans below this many samples
 STORE = {Precision.fp32: 0, Precision.fp16: 1, Precision.bf16: 2}
 TORCH_STORE = {Precision.fp32: torch.float32, Precision.fp16: torch.float16, Precision.bf16: torch.bfloat16}
 FLAG_WINDOW_OVERFLOW = 1
@@ -96,7 +96,7 @@ def _split_blocks(grid_idx: np.ndarray, xyz: np.ndarray, limit: float, out: list
 
 
 def _block_dims(spacing, shape, ndim_target=TILE):
-    """Block shape with product <= 256 balancing the physical extents."""
+    """Block shape with product <= TILE balancing the physical extents."""
     sp = [max(s, 1e-12) for s in spacing]
     dims = [1] * len(sp)
     while True:
@@ -114,7 +114,7 @@ def _block_dims(spacing, shape, ndim_target=TILE):
 
 
 def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SPAN_LIMIT) -> np.ndarray:
-    """Group pixel indices into tiles of 256 lanes (-1 = idle lane).
+    """Group pixel indices into tiles of 512 lanes (-1 = idle lane).
 
     A tile's receive and transmit delay spans are bounded by its bounding-box
     diagonal; tiles are shrunk until that diagonal is below
@@ -225,8 +225,12 @@ class FastGeometry:
         f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
         self.d_el = f32(probe.xyz)
         self.d_px = f32(scan.xyz)
-        self.tiles = plan_tiles(scan, fs, sound_speed) if tiles is None else tiles
-        self.d_tiles = torch.from_numpy(self.tiles).to(dev)
+        self.tiles = plan_tiles(scan, fs, sound_speed) if tiles is None else np.asarray(tiles, np.int32)
+        if self.tiles.ndim != 2 or self.tiles.shape[1] != TILE:
+            raise ValueError(f"tile map must be [n_tiles, {TILE}], got {self.tiles.shape}")
+        if self.tiles.size and (self.tiles.max() >= P or self.tiles.min() < -1):
+            raise ValueError("tile map holds pixel indices outside [0, P) other than -1")
+        self.d_tiles = torch.from_numpy(np.ascontiguousarray(self.tiles)).to(dev)
 
         # transmit events
         table_waves = []
