@@ -234,6 +234,33 @@ int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L
                   int64_t W, int64_t F, const ustb_das_geometry* geometry, int32_t dimension,
                   int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream);
 
+/* One request of a persistent batched launch (host struct; pointers inside as
+ * for ustb_das_fast). */
+typedef struct {
+    const void* ch;
+    int32_t storage;
+    int32_t is_complex;
+    int64_t L, N, W, F;
+    const ustb_das_geometry* geometry;
+    int32_t dimension;
+    int32_t epilogue;
+    const ustb_das_outputs* out;
+} ustb_das_request;
+
+/*
+ * Batched, persistent form of ustb_das_fast: every request is cut into
+ * (frame, tile) work items and one CTA per SM pulls items from a queue until all
+ * are done, so requests of different scans, probes, frame counts and sizes share
+ * one launch and balance across the GPU (one launch per kernel variant, i.e. per
+ * dimension / real-complex / storage / epilogue combination present).  The
+ * reference runs requests one at a time (+midprocess/das.m:77-317,
+ * +mex/source/das_cuda.cu:253-283 pipelines only frames).
+ * scratch: device memory of at least 8*(n+1) bytes; word 0 receives the
+ * USTB_FLAG_* bits of all requests (low 32 bits), words 1.. are queue counters.
+ * Stream-ordered; results are as ustb_das_fast gives them for each request.
+ */
+int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream);
+
 /*
  * Convert channel data to a device storage type: count scalars from `src`
  * (USTB_SRC_*) times `scale` into `dst` (USTB_STORE_*), e.g. int16 I/Q scanner

@@ -1,0 +1,127 @@
+"""Serving logic on the host: arrivals, admission against the HBM budget,
+batching, latency accounting (the device launch is faked; no GPU needed)."""
+import numpy as np
+import pytest
+
+from ustb_gb300 import serving
+
+
+class FakeEvent:
+    def __init__(self):
+        self.done = False
+
+    def record(self, stream=None):
+        pass
+
+    def query(self):
+        return self.done
+
+
+class FakeTensor:
+    def __init__(self, nbytes):
+        self._n = nbytes
+
+    def numel(self):
+        return self._n
+
+    def element_size(self):
+        return 1
+
+    def __getitem__(self, i):
+        class V:
+            def item(self):
+                return 0
+        return V()
+
+
+class FakeGeom:
+    P, N, W = 100, 4, 2
+
+
+@pytest.fixture
+def fake_server(monkeypatch):
+    events = []
+
+    class FakeRequest:
+        def __init__(self, *a, **k):
+            self.outputs = {"cube": None}
+
+    def fake_batch(reqs, scratch=None, stream=None):
+        return FakeTensor(8)
+
+    def fake_event():
+        e = FakeEvent()
+        events.append(e)
+        return e
+
+    monkeypatch.setattr(serving.fast, "Request", FakeRequest)
+    monkeypatch.setattr(serving.fast, "das_fast_batch", fake_batch)
+    monkeypatch.setattr(serving.torch.cuda, "Event", fake_event)
+    monkeypatch.setattr(serving.torch.cuda, "Stream", lambda dev: None)
+
+    class Ctx:
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+    monkeypatch.setattr(serving.torch.cuda, "stream", lambda s: Ctx())
+    srv = serving.Server("cpu", hbm_budget_bytes=10_000, max_batch=3, max_inflight=2)
+    srv.add_plan("a", FakeGeom())
+    return srv, events
+
+
+def job(nbytes, F=1):
+    return serving.Job("a", FakeTensor(nbytes), 1, True, F, 16, 3)
+
+
+def test_poisson_arrivals_seeded():
+    a = serving.poisson_arrivals(1000, 50.0, seed=7)
+    b = serving.poisson_arrivals(1000, 50.0, seed=7)
+    assert np.array_equal(a, b) and np.all(np.diff(a) > 0)
+    assert abs(len(a) / a[-1] - 50.0) < 5.0
+
+
+def test_batches_merge_arrived_requests_and_respect_inflight_limit(fake_server):
+    srv, events = fake_server
+    srv.budget = 20_000  # 7 jobs x (1000 B channels + 800 B output) fit
+    for _ in range(7):
+        srv.submit(job(1000))
+    srv.poll()
+    # two launches in flight of at most 3 requests each; one request waits
+    assert srv.launches == 2 and len(srv.pending) == 1
+    events[0].done = True
+    assert srv.poll() == 3
+    assert srv.launches == 3 and not srv.pending
+    for e in events:
+        e.done = True
+    srv.drain()
+    assert len(srv.completed) == 7 and srv.used == 0
+
+
+def test_admission_waits_for_budget(fake_server):
+    srv, events = fake_server
+    srv.budget = 10_000  # one 6800-byte job at a time
+    big = job(6000)
+    srv.submit(big)
+    srv.submit(job(6000))  # fits alone, not together with the first
+    srv.poll()
+    assert srv.launches == 1 and len(srv.pending) == 1
+    events[0].done = True
+    srv.poll()
+    assert srv.launches == 2
+    with pytest.raises(MemoryError):
+        srv.submit(job(20_000))
+
+
+def test_latency_stats():
+    js = []
+    for i in range(10):
+        j = serving.Job("a", None, 1, True, 2, 16, 3)
+        j.arrival, j.done = float(i), float(i) + 0.001 * (i + 1)
+        js.append(j)
+    st = serving.latency_stats(js)
+    assert st["frames"] == 20
+    assert st["p50_ms"] == pytest.approx(5.5)
+    assert st["frames_per_s"] == pytest.approx(20 / 9.01)

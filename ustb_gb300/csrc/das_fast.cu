@@ -26,6 +26,9 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 #include "phasor.cuh"
 
@@ -43,6 +46,7 @@ struct Params {
     const float* el;
     const float* px;
     const int32_t* tiles;
+    int64_t n_tiles;
     const ustb_wave* waves;
     const float* tx_delay_tab;
     const float* tx_apo_tab;
@@ -286,8 +290,9 @@ struct CtasPerSm {
     static constexpr int value = 1;  // 512 threads x 128 registers fill the register file
 };
 
+// Beamform one tile of one frame (the whole CTA participates).
 template <int MODE, bool CPLX, int ST, bool EPI>
-__global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_kernel(const Params A) {
+__device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
     constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
     constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
@@ -318,8 +323,7 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int64_t f = blockIdx.y;
-    const int32_t* tl = A.tiles + (int64_t)blockIdx.x * kTile;
+    const int32_t* tl = A.tiles + (int64_t)tile * kTile;
     // tile entries outside [0, P) are idle lanes; lane 0 names the tile's anchor pixel
     const int32_t p_own = __ldg(tl + tid);
     const bool live = p_own >= 0 && (int64_t)p_own < A.P;
@@ -766,6 +770,42 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// One launch per request: grid = (tiles, frames).
+template <int MODE, bool CPLX, int ST, bool EPI>
+__global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_kernel(const Params A) {
+    das_tile<MODE, CPLX, ST, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
+}
+
+// Persistent form: one CTA per SM pulls (request, frame, tile) work items from a
+// queue counter until the batch is done, so requests of different scans, channel
+// counts and frame counts share one launch and balance across SMs.
+constexpr int kMaxBatch = 40;
+struct BatchParams {
+    Params req[kMaxBatch];
+    int64_t first_item[kMaxBatch + 1];  // prefix sums of tiles * frames
+    int n;
+    unsigned long long* counter;        // queue head (device scratch, zeroed per launch)
+};
+
+template <int MODE, bool CPLX, int ST, bool EPI>
+__global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_constant__ BatchParams B) {
+    __shared__ long long s_item;
+    const int64_t total = B.first_item[B.n];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(B.counter, 1ull);
+        __syncthreads();
+        const int64_t item = s_item;
+        __syncthreads();
+        if (item >= total) break;
+        int r = 0;
+        while (r + 1 < B.n && B.first_item[r + 1] <= item) ++r;
+        const Params& A = B.req[r];
+        const int64_t local = item - B.first_item[r];
+        das_tile<MODE, CPLX, ST, EPI>(A, (int)(local % A.n_tiles), local / A.n_tiles);
+        __syncthreads();  // shared memory is reused by the next item
+    }
+}
+
 template <int MODE, bool CPLX, int ST, bool EPI>
 size_t smem_bytes(int64_t N, int64_t W) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
@@ -795,6 +835,48 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
     return USTB_OK;
 }
 
+template <int MODE, bool CPLX, int ST, bool EPI>
+int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long long* counter, cudaStream_t s) {
+    BatchParams B;
+    B.n = n;
+    B.counter = counter;
+    B.first_item[0] = 0;
+    size_t smem = 0;
+    for (int i = 0; i < n; ++i) {
+        B.req[i] = reqs[i];
+        B.first_item[i + 1] = B.first_item[i] + reqs[i].n_tiles * frames[i];
+        smem = std::max(smem, smem_bytes<MODE, CPLX, ST, EPI>(reqs[i].N, reqs[i].W));
+    }
+    if (B.first_item[n] == 0) return USTB_OK;
+    int dev = 0, optin = 0, sms = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "a request needs %zu bytes of shared memory per tile (limit %d)",
+                 smem, optin);
+    auto kern = das_fast_persistent<MODE, CPLX, ST, EPI>;
+    USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    USTB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
+    const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], (int64_t)sms);
+    kern<<<grid, kTile, smem, s>>>(B);
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
+template <bool CPLX, int ST>
+int dispatch_batch(int dim, int epi, const Params* reqs, const int64_t* frames, int n,
+                   unsigned long long* counter, cudaStream_t s) {
+    switch (dim) {
+        case USTB_DIM_NONE: return launch_batch<USTB_DIM_NONE, CPLX, ST, false>(reqs, frames, n, counter, s);
+        case USTB_DIM_RECEIVE: return launch_batch<USTB_DIM_RECEIVE, CPLX, ST, false>(reqs, frames, n, counter, s);
+        case USTB_DIM_TRANSMIT:
+            if constexpr (CPLX)
+                if (epi) return launch_batch<USTB_DIM_TRANSMIT, CPLX, ST, true>(reqs, frames, n, counter, s);
+            return launch_batch<USTB_DIM_TRANSMIT, CPLX, ST, false>(reqs, frames, n, counter, s);
+        default: return launch_batch<USTB_DIM_BOTH, CPLX, ST, false>(reqs, frames, n, counter, s);
+    }
+}
+
 template <bool CPLX, int ST>
 int dispatch_mode(int dim, int epi, const Params& A, int64_t nt, int64_t F, cudaStream_t s) {
     switch (dim) {
@@ -810,10 +892,13 @@ int dispatch_mode(int dim, int epi, const Params& A, int64_t nt, int64_t F, cuda
 
 }  // namespace
 
-extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
-                             int64_t W, int64_t F, const ustb_das_geometry* g, int32_t dimension,
-                             int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream) {
-    ustb::clear_error();
+// Validate one request and fill its kernel parameters.  Returns USTB_OK, or a
+// status; *empty is set when the request has no work (its outputs are already
+// handled, e.g. zero-filled).
+static int make_params(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N, int64_t W,
+                       int64_t F, const ustb_das_geometry* g, int32_t dimension, int32_t epilogue,
+                       const ustb_das_outputs* out, uint32_t* flags, cudaStream_t s, Params& A, bool& empty) {
+    empty = false;
     USTB_REQUIRE(g && out, USTB_E_ARG, "geometry and outputs must be given");
     USTB_REQUIRE(dimension >= 0 && dimension <= 3, USTB_E_ARG, "Unknown sum mode %d", (int)dimension);
     USTB_REQUIRE(storage >= 0 && storage <= 2, USTB_E_DTYPE, "unknown storage type %d", (int)storage);
@@ -829,11 +914,10 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     USTB_REQUIRE(flags, USTB_E_ARG, "flags pointer is NULL");
     USTB_REQUIRE(F <= 65535, USTB_E_SHAPE, "at most 65535 frames per call");
     USTB_REQUIRE(L <= INT32_MAX - 256, USTB_E_SHAPE, "L=%lld exceeds the 32-bit sample index", (long long)L);
+    USTB_REQUIRE(N <= 1000000 && W <= 1000000, USTB_E_SHAPE, "N and W must be below 10^6");
     USTB_REQUIRE(g->n_tiles <= INT32_MAX, USTB_E_SHAPE, "too many tiles");
     USTB_REQUIRE(g->sound_speed > 0.f && g->fs > 0.f, USTB_E_ARG, "sound speed and fs must be > 0");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    USTB_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t), s));
-    if (g->n_tiles == 0 || F == 0 || g->n_pixels == 0) return USTB_OK;
+    if (g->n_tiles == 0 || F == 0 || g->n_pixels == 0) { empty = true; return USTB_OK; }
     USTB_REQUIRE(g->element_xyz && g->pixel_xyz && g->tile_pixels && (W == 0 || g->waves), USTB_E_ARG,
                  "a geometry pointer is NULL");
     USTB_REQUIRE(L == 0 || N == 0 || W == 0 || ch, USTB_E_ARG, "channel data pointer is NULL");
@@ -843,14 +927,15 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
         const int64_t nout = out_elems(dimension, P, N, W, F);
         if (out->cube && nout)
             USTB_CUDA(cudaMemsetAsync(out->cube, 0, (size_t)nout * (is_complex ? 8 : 4), s));
+        empty = true;
         return USTB_OK;
     }
-    Params A;
     A.ch = ch;
     A.L = L; A.N = N; A.W = W; A.F = F; A.P = P;
     A.el = g->element_xyz;
     A.px = g->pixel_xyz;
     A.tiles = g->tile_pixels;
+    A.n_tiles = g->n_tiles;
     A.waves = g->waves;
     A.tx_delay_tab = g->tx_delay_table;
     A.tx_apo_tab = g->tx_apo_table;
@@ -874,6 +959,20 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     const OutStrides os = out_strides(dimension, P, N, W);
     A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
     A.flags = flags;
+    return USTB_OK;
+}
+
+extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
+                             int64_t W, int64_t F, const ustb_das_geometry* g, int32_t dimension,
+                             int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream) {
+    ustb::clear_error();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    USTB_REQUIRE(flags, USTB_E_ARG, "flags pointer is NULL");
+    USTB_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t), s));
+    Params A;
+    bool empty = false;
+    int rc = make_params(ch, storage, is_complex, L, N, W, F, g, dimension, epilogue, out, flags, s, A, empty);
+    if (rc || empty) return rc;
     const int64_t nt = g->n_tiles;
     if (is_complex) {
         switch (storage) {
@@ -887,4 +986,68 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
         case USTB_STORE_F16: return dispatch_mode<false, USTB_STORE_F16>(dimension, 0, A, nt, F, s);
         default: return dispatch_mode<false, USTB_STORE_BF16>(dimension, 0, A, nt, F, s);
     }
+}
+
+extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(n >= 0 && (n == 0 || reqs), USTB_E_ARG, "bad request array");
+    USTB_REQUIRE(scratch, USTB_E_ARG, "scratch pointer is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* flags = reinterpret_cast<uint32_t*>(scratch);
+    USTB_CUDA(cudaMemsetAsync(scratch, 0, sizeof(uint64_t), s));
+    if (n == 0) return USTB_OK;
+    // validate all requests first, then launch one persistent kernel per kernel variant
+    std::vector<Params> P(n);
+    std::vector<int64_t> frames(n);
+    std::vector<int> key(n, -1);
+    for (int i = 0; i < n; ++i) {
+        const ustb_das_request& q = reqs[i];
+        bool empty = false;
+        int rc = make_params(q.ch, q.storage, q.is_complex, q.L, q.N, q.W, q.F, q.geometry, q.dimension,
+                             q.epilogue, q.out, flags, s, P[i], empty);
+        if (rc) {
+            char msg[1200];
+            snprintf(msg, sizeof msg, "request %d: %s", i, ustb_last_error());
+            ustb::set_error("%s", msg);
+            return rc;
+        }
+        frames[i] = q.F;
+        if (!empty) key[i] = ((q.dimension * 2 + q.is_complex) * 3 + q.storage) * 2 + (q.epilogue ? 1 : 0);
+    }
+    int group = 0;
+    std::vector<bool> done(n, false);
+    for (int i = 0; i < n; ++i) {
+        if (key[i] < 0 || done[i]) continue;
+        std::vector<Params> gp;
+        std::vector<int64_t> gf;
+        for (int j = i; j < n; ++j)
+            if (!done[j] && key[j] == key[i]) {
+                gp.push_back(P[j]);
+                gf.push_back(frames[j]);
+                done[j] = true;
+            }
+        const ustb_das_request& q = reqs[i];
+        for (size_t off = 0; off < gp.size(); off += kMaxBatch) {
+            const int cnt = (int)std::min<size_t>(kMaxBatch, gp.size() - off);
+            unsigned long long* counter = reinterpret_cast<unsigned long long*>(scratch + 1 + group);
+            ++group;
+            USTB_REQUIRE(group <= n, USTB_E_ARG, "scratch holds n + 1 words");
+            int rc;
+            if (q.is_complex) {
+                switch (q.storage) {
+                    case USTB_STORE_F32: rc = dispatch_batch<true, USTB_STORE_F32>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                    case USTB_STORE_F16: rc = dispatch_batch<true, USTB_STORE_F16>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                    default: rc = dispatch_batch<true, USTB_STORE_BF16>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                }
+            } else {
+                switch (q.storage) {
+                    case USTB_STORE_F32: rc = dispatch_batch<false, USTB_STORE_F32>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                    case USTB_STORE_F16: rc = dispatch_batch<false, USTB_STORE_F16>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                    default: rc = dispatch_batch<false, USTB_STORE_BF16>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
+                }
+            }
+            if (rc) return rc;
+        }
+    }
+    return USTB_OK;
 }

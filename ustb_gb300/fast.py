@@ -57,6 +57,13 @@ class COutputs(ctypes.Structure):
                 ("cf_image", ctypes.c_void_p), ("sdmas", ctypes.c_void_p)]
 
 
+class CRequest(ctypes.Structure):
+    _fields_ = [("ch", ctypes.c_void_p), ("storage", ctypes.c_int32), ("is_complex", ctypes.c_int32),
+                ("L", ctypes.c_int64), ("N", ctypes.c_int64), ("W", ctypes.c_int64), ("F", ctypes.c_int64),
+                ("geometry", ctypes.c_void_p), ("dimension", ctypes.c_int32), ("epilogue", ctypes.c_int32),
+                ("out", ctypes.c_void_p)]
+
+
 assert ctypes.sizeof(CWave) == 48
 
 
@@ -388,3 +395,60 @@ def das_fast(ch: torch.Tensor, precision: Precision, is_complex: bool, geom: Fas
             raise _lib.UstbError(7, "a tile's sample window overflowed its slot; plan smaller tiles")
     outs["flags"] = flags
     return outs
+
+
+class Request:
+    """One beamforming request for ``das_fast_batch``: channel data already in the
+    storage type on the device, its geometry, and the outputs to fill."""
+
+    def __init__(self, ch: torch.Tensor, precision: Precision, is_complex: bool, geom: FastGeometry,
+                 dimension=Dimension.both, F: int = 1, L: Optional[int] = None, epilogue: bool = False,
+                 cube: bool = True):
+        self.ch, self.precision, self.is_complex, self.geom = ch, Precision(precision), bool(is_complex), geom
+        self.dimension, self.F, self.epilogue = int(dimension), int(F), bool(epilogue)
+        P, N, W = geom.P, geom.N, geom.W
+        self.L = int(L) if L is not None else ch.numel() // ((2 if is_complex else 1) * N * W * F)
+        dev = ch.device
+        self.outputs = {}
+        self.c_out = COutputs()
+        if cube:
+            from .kernels import out_shape_abi
+
+            dt = torch.complex64 if is_complex else torch.float32
+            self.outputs["cube"] = torch.empty(out_shape_abi(P, N, W, F, dimension), dtype=dt, device=dev)
+            self.c_out.cube = self.outputs["cube"].data_ptr()
+        if epilogue:
+            for k, dt in (("das", torch.complex64), ("cf", torch.float32), ("cf_image", torch.complex64),
+                          ("sdmas", torch.float32)):
+                self.outputs[k] = torch.empty((F, P), dtype=dt, device=dev)
+            self.c_out.das, self.c_out.cf = self.outputs["das"].data_ptr(), self.outputs["cf"].data_ptr()
+            self.c_out.cf_image = self.outputs["cf_image"].data_ptr()
+            self.c_out.sdmas = self.outputs["sdmas"].data_ptr()
+
+    def c_struct(self) -> CRequest:
+        q = CRequest()
+        q.ch = self.ch.data_ptr()
+        q.storage = STORE[self.precision]
+        q.is_complex = int(self.is_complex)
+        q.L, q.N, q.W, q.F = self.L, self.geom.N, self.geom.W, self.F
+        q.geometry = ctypes.addressof(self.geom.c)
+        q.dimension = self.dimension
+        q.epilogue = int(self.epilogue)
+        q.out = ctypes.addressof(self.c_out)
+        return q
+
+
+def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] = None, stream=None):
+    """Beamform a batch of requests with the persistent work-queue kernel
+    (``ustb_das_fast_batch``).  Returns the int64 scratch tensor (word 0 = flags)."""
+    if not requests:
+        return scratch
+    dev = requests[0].ch.device
+    n = len(requests)
+    if scratch is None or scratch.numel() < n + 1:
+        scratch = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    arr = (CRequest * n)(*[r.c_struct() for r in requests])
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    with torch.cuda.device(dev):
+        _lib.call("ustb_das_fast_batch", ctypes.addressof(arr), n, scratch.data_ptr(), st)
+    return scratch

@@ -388,3 +388,74 @@ class Apodization:
                 B[i + j * (nl // mla[0])] = correlate2d(sh, k, mode="same")
         out = np.broadcast_to(B.transpose(1, 2, 0)[None], (nd, nl, ny, W))
         return out.reshape(nd * nl * ny, W, order="F").copy()
+
+
+# ---------------------------------------------------------------------------
+# the same receive tables built on the GPU (large scans)
+# ---------------------------------------------------------------------------
+
+def _window_torch(window: Window, r):
+    import torch
+
+    w = Window(int(window))
+    if w == Window.boxcar:
+        return (r <= 0.5).to(r.dtype)
+    if w == Window.hanning:
+        return (r <= 0.5) * (0.5 + 0.5 * torch.cos(2 * math.pi * r))
+    if w == Window.hamming:
+        return (r <= 0.5) * (0.53836 + 0.46164 * torch.cos(2 * math.pi * r))
+    if w in (Window.tukey25, Window.tukey50, Window.tukey75):
+        roll = {Window.tukey25: 0.25, Window.tukey50: 0.5, Window.tukey75: 0.75}[w]
+        return ((r <= 0.5 * (1 - roll)).to(r.dtype)
+                + (r > 0.5 * (1 - roll)) * (r < 0.5) * 0.5 * (1 + torch.cos(2 * math.pi / roll * (r - roll / 2 - 0.5))))
+    if w == Window.triangle:
+        return (r <= 0.5) * (1 - 2 * r)
+    raise ValueError("Unknown apodization type!")
+
+
+def receive_tables_device(probe: Probe, scan: Scan, sound_speed: float, apo: "Apodization",
+                          lens_delay: float = 0.0, device="cuda", chunk: int = 64):
+    """Single-precision receive delay and apodization tables in the ABI layout
+    (N, P), computed on ``device`` in double precision with the formulas of
+    ``receive_delay`` and ``Apodization.aperture_apodization`` (windows, flat
+    probes, no tilt, optional origin)."""
+    import torch
+
+    dev = torch.device(device)
+    P, N = scan.N_pixels, probe.N_elements
+    px = torch.as_tensor(scan.xyz, dtype=torch.float64, device=dev)
+    el = torch.as_tensor(probe.xyz, dtype=torch.float64, device=dev)
+    dly = torch.empty((N, P), dtype=torch.float32, device=dev)
+    ap = torch.empty((N, P), dtype=torch.float32, device=dev)
+    origin = apo.origin
+    if origin is None and isinstance(scan, SectorScan):
+        origin = scan.origin
+    for n0 in range(0, N, chunk):
+        e = el[n0:n0 + chunk]  # [c, 3]
+        d = px[None, :, :] - e[:, None, :]  # pixel - element, [c, P, 3]
+        dly[n0:n0 + chunk] = (torch.linalg.norm(d, dim=2) / sound_speed + lens_delay).float()
+        if apo.apodization_vector is not None or apo.window in (Window.sta, Window.scanline) or apo.tilt != (0.0, 0.0):
+            raise ValueError("device tables cover windowed apodization without tilt")
+        if apo.window == Window.none:
+            ap[n0:n0 + chunk] = 1.0
+            continue
+        if origin is not None:
+            o = torch.tensor([origin.x, origin.y, origin.z], dtype=torch.float64, device=dev)
+            xd = (e[:, 0] - o[0])[:, None].expand(-1, P)
+            yd = (e[:, 1] - o[1])[:, None].expand(-1, P)
+            zd = torch.linalg.norm(px - o, dim=1)[None, :].expand(e.shape[0], -1)
+        else:
+            xd, yd, zd = d[..., 0], d[..., 1], d[..., 2]
+        a = zd.abs()
+        zz = []
+        for i in range(2):
+            z = zd.clone()
+            lo = apo.minimum_aperture[i] * apo.f_number[i]
+            hi = apo.maximum_aperture[i] * apo.f_number[i]
+            z = torch.where(a <= lo, torch.sign(zd) * lo, z)
+            z = torch.where(a >= hi, torch.sign(zd) * hi, z)
+            zz.append(z)
+        rt = (apo.f_number[0] * xd / zz[0]).abs()
+        rp = (apo.f_number[1] * yd / zz[1]).abs()
+        ap[n0:n0 + chunk] = (_window_torch(apo.window, rt) * _window_torch(apo.window, rp)).float()
+    return dly, ap

@@ -1,0 +1,180 @@
+"""Continuous-batching beamforming server on one GPU.
+
+Requests of different probes, scans and sizes arrive over time.  The server
+keeps each shape's geometry (``FastGeometry``: element and pixel positions,
+transmit events, tile map) resident on the device, admits arrived requests
+while their buffers fit an HBM budget, and merges everything admitted into the
+next persistent launch (``ustb_das_fast_batch``).  Up to ``max_inflight``
+launches overlap on the device: requests that arrive while a batch runs join
+the next one instead of waiting for the GPU to drain.  Latency is measured from
+arrival to the completion event of the request's batch.
+
+The reference has no serving layer: midprocess.das beamforms one dataset per
+call (+midprocess/das.m:77-317).
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import fast
+from .enums import Precision
+
+
+@dataclass
+class Job:
+    """A request in flight: channel data (device, storage type), its shape key and frames."""
+    key: str
+    ch: torch.Tensor
+    precision: Precision
+    is_complex: bool
+    F: int
+    L: int
+    dimension: int
+    epilogue: bool = False
+    arrival: float = 0.0
+    admitted: float = 0.0
+    done: float = 0.0
+    outputs: Dict[str, torch.Tensor] = field(default_factory=dict)
+    reserved: int = 0
+    callback: Optional[Callable[["Job"], None]] = None
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+class Server:
+    """Event-loop server: ``submit`` jobs, call ``poll`` (or ``run``) to make progress."""
+
+    def __init__(self, device, hbm_budget_bytes: float = 150e9, max_batch: int = 32, max_inflight: int = 2):
+        self.device = torch.device(device)
+        self.budget = int(hbm_budget_bytes)
+        self.used = 0
+        self.max_batch = max_batch
+        self.max_inflight = max_inflight
+        self.plans: Dict[str, fast.FastGeometry] = {}
+        self.pending: collections.deque = collections.deque()
+        self.inflight: List = []  # (event, jobs, requests, scratch)
+        self.completed: List[Job] = []
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(max_inflight)]
+        self._next_stream = 0
+        self.launches = 0
+
+    # -- plans -------------------------------------------------------------------
+    def add_plan(self, key: str, geom: fast.FastGeometry) -> None:
+        self.plans[key] = geom
+
+    # -- requests ----------------------------------------------------------------
+    def _bytes(self, job: Job) -> int:
+        g = self.plans[job.key]
+        out = g.P * job.F * (8 if job.is_complex else 4)
+        if job.dimension in (0, 2):
+            out *= g.N
+        if job.dimension in (0, 1):
+            out *= g.W
+        return int(job.ch.numel() * job.ch.element_size() + out)
+
+    def submit(self, job: Job, now: Optional[float] = None) -> Job:
+        if job.key not in self.plans:
+            raise KeyError(f"no plan for shape {job.key!r}: add_plan first")
+        job.arrival = time.perf_counter() if now is None else now
+        job.reserved = self._bytes(job)
+        if job.reserved > self.budget:
+            raise MemoryError(f"request needs {job.reserved} bytes, budget is {self.budget}")
+        self.pending.append(job)
+        return job
+
+    def _launch(self) -> None:
+        batch: List[Job] = []
+        while self.pending and len(batch) < self.max_batch:
+            job = self.pending[0]
+            if self.used + job.reserved > self.budget:
+                break
+            self.pending.popleft()
+            self.used += job.reserved
+            batch.append(job)
+        if not batch:
+            return
+        t = time.perf_counter()
+        stream = self.streams[self._next_stream]
+        self._next_stream = (self._next_stream + 1) % len(self.streams)
+        reqs = []
+        with torch.cuda.stream(stream):
+            for job in batch:
+                job.admitted = t
+                cube = not job.epilogue
+                r = fast.Request(job.ch, job.precision, job.is_complex, self.plans[job.key], job.dimension,
+                                 F=job.F, L=job.L, epilogue=job.epilogue, cube=cube)
+                job.outputs = r.outputs
+                reqs.append(r)
+            scratch = fast.das_fast_batch(reqs, stream=stream)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        self.inflight.append((ev, batch, reqs, scratch))
+        self.launches += 1
+
+    def poll(self) -> int:
+        """Retire finished batches and launch new ones.  Returns jobs completed now."""
+        n = 0
+        still = []
+        for ev, batch, reqs, scratch in self.inflight:
+            if ev.query():
+                t = time.perf_counter()
+                flags = int(scratch[0].item()) & 0xFFFFFFFF
+                for job in batch:
+                    job.done = t
+                    self.used -= job.reserved
+                    if flags & fast.FLAG_WINDOW_OVERFLOW:
+                        job.outputs["error"] = "window overflow"
+                    self.completed.append(job)
+                    if job.callback:
+                        job.callback(job)
+                n += len(batch)
+            else:
+                still.append((ev, batch, reqs, scratch))
+        self.inflight = still
+        while self.pending and len(self.inflight) < self.max_inflight:
+            before = len(self.pending)
+            self._launch()
+            if len(self.pending) == before:
+                break
+        return n
+
+    def drain(self) -> None:
+        while self.pending or self.inflight:
+            self.poll()
+
+    # -- replay a timed arrival stream -------------------------------------------
+    def run(self, arrivals: List[float], make_job: Callable[[int], Job]) -> List[Job]:
+        """Submit job i at time start + arrivals[i] (seconds) and serve until all are done."""
+        jobs = [make_job(i) for i in range(len(arrivals))]
+        start = time.perf_counter()
+        i = 0
+        while i < len(jobs) or self.pending or self.inflight:
+            now = time.perf_counter() - start
+            while i < len(jobs) and arrivals[i] <= now:
+                self.submit(jobs[i], start + arrivals[i])
+                i += 1
+            self.poll()
+        return jobs
+
+
+def poisson_arrivals(n: int, rate_hz: float, seed: int) -> np.ndarray:
+    """Arrival times (s) of a Poisson stream of ``n`` requests."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_hz, n))
+
+
+def latency_stats(jobs: List[Job]) -> Dict[str, float]:
+    lat = np.array([j.latency for j in jobs]) * 1e3
+    frames = sum(j.F for j in jobs)
+    span = max(j.done for j in jobs) - min(j.arrival for j in jobs)
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "frames": int(frames), "seconds": float(span),
+            "frames_per_s": float(frames / span)}
