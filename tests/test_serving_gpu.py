@@ -67,7 +67,8 @@ def test_server_results_same_alone_and_in_mix(workloads, cuda_dev):
         srv.add_plan(name, geom)
     names = list(workloads)
     order = [names[i % len(names)] for i in range(12)]
-    arrivals = serving.poisson_arrivals(len(order), 2000.0, seed=3)
+    # a burst: everything arrives while the first launch is still on the GPU
+    arrivals = serving.poisson_arrivals(len(order), 1e7, seed=3)
 
     def make(i):
         wl, geom, st, prec, cplx, L = workloads[order[i]]
