@@ -227,27 +227,51 @@ def serving_mix(device, n_requests, seed, torch):
         a = plain[k]
         kernels.das_table_f32(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8])
 
-    # plain single-request FP32 DAS: requests one after another
+    def ev_ms(fn, n=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    per_kind = {}
     for k in kinds:
-        run_plain(k)
+        wl, das, ch, st, cplx = prep[k]
+        epi = wl.epilogue is not None
+        per_kind[k] = {
+            "plain_fp32_ms": round(ev_ms(lambda: run_plain(k)), 3),
+            "fast_fp16_ms": round(ev_ms(lambda: fast.das_fast(st, Precision.fp16, cplx, srv.plans[k], wl.dimension,
+                                                               L=ch.shape[-1], epilogue=epi, cube=not epi,
+                                                               check=False)), 3),
+            "units": wl.units}
+    # plain single-request FP32 DAS: the requests one after another
     torch.cuda.synchronize()
     t = time.perf_counter()
     for k in order:
         run_plain(k)
         torch.cuda.synchronize()
     plain_s = time.perf_counter() - t
-    # served: capacity-limited stream (rate above the plain path's request rate)
-    rate = 4.0 * n_requests / plain_s
 
-    def make(i):
+    def make(i, order=order):
         k = order[i]
         wl, das, ch, st, cplx = prep[k]
         return serving.Job(k, st, Precision.fp16, cplx, 1, ch.shape[-1], int(wl.dimension),
                            epilogue=wl.epilogue is not None)
 
-    srv.run(list(serving.poisson_arrivals(8, rate, seed + 1)), make)  # warm-up
+    srv.run([0.0] * 8, make)  # warm-up
+    # saturated throughput: the whole stream arrives at once
     srv.completed.clear()
     launches0 = srv.launches
+    burst = srv.run([0.0] * n_requests, make)
+    sat = serving.latency_stats(burst)
+    launches = srv.launches - launches0
+    # latency: Poisson arrivals at 70 % of the saturated request rate
+    rate = 0.7 * n_requests / sat["seconds"]
+    srv.completed.clear()
     jobs = srv.run(list(serving.poisson_arrivals(n_requests, rate, seed)), make)
     stats = serving.latency_stats(jobs)
     # accuracy of each kind against the FP64 oracle on a pixel subset
@@ -283,14 +307,16 @@ def serving_mix(device, n_requests, seed, torch):
         errs[k] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
     return {
         "requests": n_requests, "kinds": kinds, "seed": seed,
-        "served_frames_per_s": round(stats["frames_per_s"], 1),
-        "p50_ms": round(stats["p50_ms"], 3), "p99_ms": round(stats["p99_ms"], 3),
+        "served_frames_per_s": round(sat["frames_per_s"], 1),
         "plain_fp32_frames_per_s": round(n_requests / plain_s, 1),
-        "speedup_vs_plain": round(stats["frames_per_s"] / (n_requests / plain_s), 2),
-        "launches": srv.launches - launches0, "arrival_rate_hz": round(rate, 1),
-        "hbm_budget_gb": 150, "storage": "fp16 (int16 -> fp16 for int16 sources)",
+        "speedup_vs_plain": round(sat["frames_per_s"] / (n_requests / plain_s), 2),
+        "launches_for_stream": launches,
+        "latency_at_70pct_load": {"arrival_rate_hz": round(rate, 1), "p50_ms": round(stats["p50_ms"], 3),
+                                  "p99_ms": round(stats["p99_ms"], 3), "frames_per_s": round(stats["frames_per_s"], 1)},
+        "per_kind": per_kind,
+        "hbm_budget_gb": 150, "storage": "fp16",
         "rel_l2_vs_fp64_oracle": {k: float(f"{v:.3g}") for k, v in errs.items()},
-        "plain_path": "ustb_das_table_f32 (das_c-exact FP32 tables), one request at a time",
+        "plain_path": "ustb_das_table_f32 (das_c-exact FP32 tables resident), one request at a time",
     }
 
 

@@ -27,6 +27,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -669,20 +670,26 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
             const int n0 = stage_n0(si);
             run_stage(si);
             setup_rx(n0);
+            const int kw = min(KW, (int)W - cur * KW);
+            auto units = [&](auto full) {
 #pragma unroll
-            for (int c = 0; c < CG; ++c) {
-                const float2 b = B[c];
+                for (int c = 0; c < CG; ++c) {
+                    const float2 b = B[c];
 #pragma unroll
-                for (int k = 0; k < KW; ++k) {
-                    const float2 v = interp(c, k, stx[k] + srx[c]);
-                    if constexpr (CPLX) {
-                        accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
-                        acci[k] = fmaf(b.x, v.y, fmaf(b.y, v.x, acci[k]));
-                    } else {
-                        accr[k] = fmaf(b.x, v.x, accr[k]);
+                    for (int k = 0; k < KW; ++k) {
+                        if (!decltype(full)::value && k >= kw) continue;  // last, partial wave chunk
+                        const float2 v = interp(c, k, stx[k] + srx[c]);
+                        if constexpr (CPLX) {
+                            accr[k] = fmaf(b.x, v.x, fmaf(-b.y, v.y, accr[k]));
+                            acci[k] = fmaf(b.x, v.y, fmaf(b.y, v.x, acci[k]));
+                        } else {
+                            accr[k] = fmaf(b.x, v.x, accr[k]);
+                        }
                     }
                 }
-            }
+            };
+            if (kw == KW) units(std::true_type{});
+            else units(std::false_type{});
         }
         if (cur >= 0) finish_chunk();
         zero_chunks(cur + 1, NC);

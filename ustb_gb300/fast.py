@@ -184,6 +184,30 @@ def refine_tiles(tiles: np.ndarray, xyz: np.ndarray, tx_samples: np.ndarray,
     return _pack(out)
 
 
+def order_by_cost(tiles: np.ndarray, xyz: np.ndarray, probe_xyz: np.ndarray, rx: "Apodization") -> np.ndarray:
+    """Reorder tiles most-expensive first.  A tile's cost is the number of
+    channels whose receive window can be nonzero somewhere in the tile (the
+    kernel's own bounding-box rule), so the block scheduler hands the long tiles
+    out first and the short ones fill the tail."""
+    if len(tiles) < 2 or rx is None or rx.window == Window.none or rx.apodization_vector is not None:
+        return tiles
+    lo = np.empty((len(tiles), 3))
+    hi = np.empty((len(tiles), 3))
+    for t, row in enumerate(tiles):
+        b = xyz[row[row >= 0]]
+        lo[t], hi[t] = b.min(0), b.max(0)
+    ex, ey, ez = probe_xyz[:, 0][None, :], probe_xyz[:, 1][None, :], probe_xyz[:, 2][None, :]
+    xd = np.maximum(0, np.maximum(lo[:, 0:1] - ex, ex - hi[:, 0:1]))
+    yd = np.maximum(0, np.maximum(lo[:, 1:2] - ey, ey - hi[:, 1:2]))
+    zmax = np.maximum(np.abs(lo[:, 2:3] - ez), np.abs(hi[:, 2:3] - ez))
+    zx = np.clip(zmax, rx.minimum_aperture[0] * rx.f_number[0], rx.maximum_aperture[0] * rx.f_number[0])
+    zy = np.clip(zmax, rx.minimum_aperture[1] * rx.f_number[1], rx.maximum_aperture[1] * rx.f_number[1])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        act = ~((rx.f_number[0] * xd / zx > 0.5) | (rx.f_number[1] * yd / zy > 0.5))
+    cost = act.sum(axis=1)
+    return tiles[np.argsort(-cost, kind="stable")]
+
+
 def _pack(blocks) -> np.ndarray:
     T = len(blocks)
     tiles = np.full((T, TILE), -1, dtype=np.int32)
@@ -232,7 +256,12 @@ class FastGeometry:
         f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
         self.d_el = f32(probe.xyz)
         self.d_px = f32(scan.xyz)
-        self.tiles = plan_tiles(scan, fs, sound_speed) if tiles is None else np.asarray(tiles, np.int32)
+        if tiles is None:
+            self.tiles = plan_tiles(scan, fs, sound_speed)
+            if rx.origin is None and not isinstance(scan, SectorScan):
+                self.tiles = order_by_cost(self.tiles, scan.xyz, probe.xyz, rx)
+        else:
+            self.tiles = np.asarray(tiles, np.int32)
         if self.tiles.ndim != 2 or self.tiles.shape[1] != TILE:
             raise ValueError(f"tile map must be [n_tiles, {TILE}], got {self.tiles.shape}")
         if self.tiles.size and (self.tiles.max() >= P or self.tiles.min() < -1):
