@@ -55,6 +55,7 @@ struct Params {
     const float2* pix_phase;
     float fs, t0, fd, inv_c, lens;
     int rx_window;
+    float win_r1, win_a, win_e, win_b, win_c, win_d;  // see window_coeffs()
     float fnx, fny, minx, miny, maxx, maxy;
     int rx_origin;
     float ox, oy, oz;
@@ -70,38 +71,50 @@ struct Params {
 
 // ---------------------------------------------------------------------------
 // apodization windows, +uff/apodization.m:172-223 (0 beyond ratio 1/2)
+//
+// Every window has the form
+//   w(r) = 1                                  for r <= r1
+//        = a + e*r + b*cos(c*(r - d))          for r1 < r <= 1/2
+//        = 0                                   beyond
+// with per-window constants (window_coeffs), so the kernel evaluates it without
+// branching on the window type:
+//   boxcar    r1 = 1/2
+//   hanning   r1 = -1, a = b = 1/2, c = 2*pi, d = 0
+//   hamming   r1 = -1, a = 0.53836, b = 0.46164, c = 2*pi, d = 0
+//   tukey(R)  r1 = (1-R)/2, a = b = 1/2, c = 2*pi/R, d = R/2 + 1/2
+//   triangle  r1 = -1, a = 1, e = -2
+// (Tukey's strict r < 1/2 edge gives the same value, 0, at r = 1/2.)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float tukey(float r, float roll) {
-    const float lo = 0.5f * (1.f - roll);
-    if (r <= lo) return 1.f;
-    if (r > lo && r < 0.5f) return 0.5f * (1.f + __cosf(6.283185307179586f / roll * (r - roll * 0.5f - 0.5f)));
-    return 0.f;
+struct WinCoeffs {
+    float r1, a, e, b, c, d;
+};
+
+static WinCoeffs window_coeffs(int win) {
+    const float twopi = 6.283185307179586f;
+    switch (win) {
+        case USTB_WIN_BOXCAR: return {0.5f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        case USTB_WIN_HANNING: return {-1.f, 0.5f, 0.f, 0.5f, twopi, 0.f};
+        case USTB_WIN_HAMMING: return {-1.f, 0.53836f, 0.f, 0.46164f, twopi, 0.f};
+        case USTB_WIN_TUKEY25: return {0.375f, 0.5f, 0.f, 0.5f, twopi / 0.25f, 0.625f};
+        case USTB_WIN_TUKEY50: return {0.25f, 0.5f, 0.f, 0.5f, twopi / 0.5f, 0.75f};
+        case USTB_WIN_TUKEY75: return {0.125f, 0.5f, 0.f, 0.5f, twopi / 0.75f, 0.875f};
+        case USTB_WIN_TRIANGLE: return {-1.f, 1.f, -2.f, 0.f, 0.f, 0.f};
+        default: return {3.4e38f, 0.f, 0.f, 0.f, 0.f, 0.f};  // none: 1 everywhere
+    }
 }
 
-__device__ __forceinline__ float window(int win, float r) {
-    switch (win) {
-        case USTB_WIN_NONE: return 1.f;
-        case USTB_WIN_BOXCAR: return r <= 0.5f ? 1.f : 0.f;
-        case USTB_WIN_HANNING: return r <= 0.5f ? 0.5f + 0.5f * __cosf(6.283185307179586f * r) : 0.f;
-        case USTB_WIN_HAMMING: return r <= 0.5f ? 0.53836f + 0.46164f * __cosf(6.283185307179586f * r) : 0.f;
-        case USTB_WIN_TUKEY25: return tukey(r, 0.25f);
-        case USTB_WIN_TUKEY50: return tukey(r, 0.50f);
-        case USTB_WIN_TUKEY75: return tukey(r, 0.75f);
-        case USTB_WIN_TRIANGLE: return r <= 0.5f ? 1.f - 2.f * r : 0.f;
-        default: return 0.f;
-    }
+__device__ __forceinline__ float window(const Params& A, float r) {
+    const float taper = fmaf(A.win_e, r, A.win_a) + A.win_b * __cosf(A.win_c * (r - A.win_d));
+    const float w = r <= 0.5f ? taper : 0.f;
+    return r <= A.win_r1 ? 1.f : w;  // NaN ratios (0/0) give 0
 }
 
 __device__ __forceinline__ float msign(float v) { return (float)((v > 0.f) - (v < 0.f)); }
 
 // min/max aperture clamps of apodization.m:452-462 (MATLAB sign(0) = 0)
 __device__ __forceinline__ float clamp_ap(float z, float fnum, float minap, float maxap) {
-    const float a = fabsf(z);
-    const float lo = minap * fnum, hi = maxap * fnum;
-    float r = z;
-    if (a <= lo) r = msign(z) * lo;
-    if (a >= hi) r = msign(z) * hi;
-    return r;
+    const float a = fminf(fmaxf(fabsf(z), minap * fnum), maxap * fnum);
+    return copysignf(a, z) * (z != 0.f ? 1.f : 0.f);
 }
 
 __device__ __forceinline__ float rx_apodization(const Params& A, float ex, float ey, float ez, float px,
@@ -120,11 +133,11 @@ __device__ __forceinline__ float rx_apodization(const Params& A, float ex, float
     }
     const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
     const float rt = fabsf(A.fnx * __fdividef(xd, zx));
-    const float wx = window(A.rx_window, rt);
-    if (yd == 0.f) return wx * window(A.rx_window, 0.f);  // 1-D arrays: elevation ratio 0
+    const float wx = window(A, rt);
+    if (yd == 0.f) return wx;  // elevation ratio 0: every window is 1 there
     const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
     const float rp = fabsf(A.fny * __fdividef(yd, zy));
-    return wx * window(A.rx_window, rp);
+    return wx * window(A, rp);
 }
 
 // exp(i 2 pi fd tau) from the phase in cycles
@@ -952,6 +965,10 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
     A.inv_c = 1.f / g->sound_speed;
     A.lens = g->lens_delay;
     A.rx_window = g->rx_window;
+    {
+        const WinCoeffs wc = window_coeffs(g->rx_window);
+        A.win_r1 = wc.r1; A.win_a = wc.a; A.win_e = wc.e; A.win_b = wc.b; A.win_c = wc.c; A.win_d = wc.d;
+    }
     A.fnx = g->rx_f_number[0]; A.fny = g->rx_f_number[1];
     A.minx = g->rx_min_aperture[0]; A.miny = g->rx_min_aperture[1];
     A.maxx = g->rx_max_aperture[0]; A.maxy = g->rx_max_aperture[1];
