@@ -125,3 +125,18 @@ def test_latency_stats():
     assert st["frames"] == 20
     assert st["p50_ms"] == pytest.approx(5.5)
     assert st["frames_per_s"] == pytest.approx(20 / 9.01)
+
+
+def test_large_requests_launch_alone(fake_server):
+    srv, events = fake_server
+    srv.budget = 1e9
+    srv.large_units = 500  # FakeGeom: 100 px x 4 ch x 2 waves = 800 units per frame
+    srv.submit(serving.Job("a", FakeTensor(100), 1, True, 1, 16, 3))  # large (800)
+    small = FakeGeom()
+    small.P = 10
+    srv.add_plan("s", small)
+    for _ in range(3):
+        srv.submit(serving.Job("s", FakeTensor(100), 1, True, 1, 16, 3))  # 80 units each
+    srv.poll()
+    # the large job went alone, the three small ones together in the second launch
+    assert srv.launches == 2 and not srv.pending

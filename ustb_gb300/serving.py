@@ -52,8 +52,12 @@ class Job:
 class Server:
     """Event-loop server: ``submit`` jobs, call ``poll`` (or ``run``) to make progress."""
 
-    def __init__(self, device, hbm_budget_bytes: float = 150e9, max_batch: int = 32, max_inflight: int = 2):
+    def __init__(self, device, hbm_budget_bytes: float = 150e9, max_batch: int = 32, max_inflight: int = 2,
+                 large_units: float = 2e9):
         self.device = torch.device(device)
+        # requests with more pixel-channel-wave units than this launch on their own,
+        # so that small requests never wait for a large one sharing their launch
+        self.large_units = large_units
         self.budget = int(hbm_budget_bytes)
         self.used = 0
         self.max_batch = max_batch
@@ -90,15 +94,31 @@ class Server:
         self.pending.append(job)
         return job
 
+    def _units(self, job: Job) -> int:
+        g = self.plans[job.key]
+        return g.P * g.N * g.W * job.F
+
     def _launch(self) -> None:
+        """Admit pending jobs in arrival order into one launch: either a single large
+        job, or as many small jobs as fit the budget and the batch size."""
         batch: List[Job] = []
+        large_first = bool(self.pending) and self._units(self.pending[0]) > self.large_units
+        skipped = collections.deque()
         while self.pending and len(batch) < self.max_batch:
-            job = self.pending[0]
-            if self.used + job.reserved > self.budget:
-                break
-            self.pending.popleft()
+            job = self.pending.popleft()
+            large = self._units(job) > self.large_units
+            if (large and batch) or (large_first and batch) or self.used + job.reserved > self.budget:
+                skipped.append(job)
+                if large_first or self.used + job.reserved > self.budget:
+                    break
+                continue
             self.used += job.reserved
             batch.append(job)
+            if large:
+                break
+        # jobs passed over keep their place at the front of the queue
+        while skipped:
+            self.pending.appendleft(skipped.pop())
         if not batch:
             return
         t = time.perf_counter()
