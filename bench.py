@@ -50,6 +50,9 @@ UNIT = "G pixel·channel·wave/s"
 FLOP_PER_UNIT_IQ = 22  # algorithmic FP32 FLOP per IQ unit (+2 MUFU sincos)
 FLOP_PER_UNIT_RF = 10
 FP32_LANES_PER_SM = 128
+# DRAM bytes (read + write) of one das_fast_kernel<both, complex, f32> launch on the
+# headline workload, from an ncu capture of `bench.py --profile headline`
+TRAFFIC_FAST_F32_HEADLINE = 75_910_144
 
 
 def measured_peaks():
@@ -330,7 +333,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-requests", type=int, default=200)
+    ap.add_argument("--profile", default=None, metavar="WORKLOAD",
+                    help="launch only the kernels of one workload (headline or a synth.CONFIGS name) "
+                         "--steps times each, for ncu; prints their CUDA-event times")
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "bf16"],
+                    help="channel storage of the fast kernel under --profile")
     args = ap.parse_args()
+    if args.profile:
+        return main_profile(args)
 
     import torch
 
@@ -432,6 +442,8 @@ def main():
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
     achieved = FLOP_PER_UNIT_IQ * act / (ms * 1e-3) / 1e12
+    # compulsory bytes of the fast path: channel data, image, pixel xyz, tile map
+    h_bytes_alg = (ch.numel() * ch.element_size() + P * F * 8 + P * 12 + geom.tiles.size * 4)
     res = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": warm, "ms_per_step": round(ms, 4),
@@ -451,7 +463,9 @@ def main():
         },
         "roofline": {
             "bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
-            "frac": round(achieved / fp32_peak, 4), "traffic": None,
+            "frac": round(achieved / fp32_peak, 4), "traffic": TRAFFIC_FAST_F32_HEADLINE,
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch)",
+            "algorithmic_bytes": int(h_bytes_alg),
             "kernel": "das_fast_kernel<both, complex, f32>",
             "flop_per_unit": FLOP_PER_UNIT_IQ, "units_counted": "das_c_active_units (nonzero tx x rx apodization)",
             "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max:.0f} "
@@ -470,6 +484,60 @@ def main():
         ch_np = kernels.to_matlab_order(ch).cpu().numpy()
         res["cpu_baseline"] = cpu_reference(ch_np, fs, t0, fd, tabs, 3)
     print(json.dumps(res), flush=True)
+
+
+def main_profile(args):
+    """A short run for ncu: the fast kernel, then the das_c-exact table kernel, on one
+    workload, ``--steps`` launches each after ``--warmup`` warm-up launches each."""
+    import torch
+
+    from ustb_gb300 import fast, geometry, kernels, synth
+    from ustb_gb300.enums import Precision
+
+    dev = torch.device("cuda", 0)
+    if args.profile == "headline":
+        wl, das, ch = make_headline(dev)
+    else:
+        from ustb_gb300.das import channel_tensor
+
+        wl = synth.CONFIGS[args.profile](device=dev)
+        das = build_das(wl)
+        ch = channel_tensor(wl.channel_data.data, dev)
+    cd = wl.channel_data
+    prec = Precision[args.storage]
+    cplx = ch.is_complex()
+    epi = wl.epilogue is not None
+    geom = das.fast_geometry(dev)
+    st = fast.convert_channels(ch, prec)
+    flags = torch.zeros(1, dtype=torch.int32, device=dev)
+    L = ch.shape[-1]
+
+    def fast_step():
+        fast.das_fast(st, prec, cplx, geom, int(wl.dimension), L=L, epilogue=epi, cube=not epi, flags=flags,
+                      check=False)
+
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
+    txa = das.transmit_apodization.wave_apodization(cd.sequence, wl.scan).astype(np.float32)
+    txd = geometry.transmit_delay(cd.sequence, wl.scan).astype(np.float32)
+    rxd, rxa = geometry.receive_tables_device(cd.probe, wl.scan, cd.sound_speed, das.receive_apodization,
+                                              device=dev)
+    fs, t0, fd = (float(np.float32(cd.sampling_frequency)), float(np.float32(cd.initial_time)),
+                  float(np.float32(cd.modulation_frequency)))
+    d_txa, d_txd = T(txa), T(txd)
+
+    def table_step():
+        kernels.das_table_f32(ch, fs, t0, d_txa, rxa, d_txd, rxd, fd, int(wl.dimension))
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"profile": args.profile, "storage": args.storage, "units": wl.units}
+    for name, fn in (("fast", fast_step), ("table", table_step)):
+        for _ in range(args.warmup):
+            fn()
+        out[name + "_ms"] = [round(t, 4) for t in cuda_time(fn, args.steps, flush, stream, torch)]
+    torch.cuda.synchronize()
+    out["window_overflow"] = int(flags.item())
+    print(json.dumps(out), flush=True)
 
 
 def main_reference(args, rank, world):
