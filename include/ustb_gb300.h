@@ -229,6 +229,10 @@ typedef struct {
  * without writing the channel cube (out->cube may be NULL).
  * flags: device uint32, cleared by the call; USTB_FLAG_WINDOW_OVERFLOW means a
  * tile was too large for its sample windows (re-plan with smaller tiles).
+ * The call first rewrites the channel data as FP32 interpolation entries
+ * {x_i, x_(i+1) - x_i} (16 bytes per complex sample, 8 per real one) in a
+ * stream-ordered scratch array that the library allocates from its own memory
+ * pool and frees before returning (USTB_E_OOM when it does not fit).
  */
 int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
                   int64_t W, int64_t F, const ustb_das_geometry* geometry, int32_t dimension,
@@ -252,7 +256,8 @@ typedef struct {
  * (frame, tile) work items and one CTA per SM pulls items from a queue until all
  * are done, so requests of different scans, probes, frame counts and sizes share
  * one launch and balance across the GPU (one launch per kernel variant, i.e. per
- * dimension / real-complex / storage / epilogue combination present).  The
+ * dimension / real-complex / epilogue combination present).  Each request's
+ * entry array (see ustb_das_fast) lives in library scratch until the launches are done.  The
  * reference runs requests one at a time (+midprocess/das.m:77-317,
  * +mex/source/das_cuda.cu:253-283 pipelines only frames).
  * scratch: device memory of at least 8*(n+1) bytes; word 0 receives the

@@ -85,7 +85,7 @@ def test_poisson_arrivals_seeded():
 
 def test_batches_merge_arrived_requests_and_respect_inflight_limit(fake_server):
     srv, events = fake_server
-    srv.budget = 20_000  # 7 jobs x (1000 B channels + 800 B output) fit
+    srv.budget = 30_000  # 7 jobs x (1000 B channels + 800 B output + 2048 B entries) fit
     for _ in range(7):
         srv.submit(job(1000))
     srv.poll()

@@ -9,12 +9,17 @@
 //   A_w = apo_tx * exp(i 2 pi fd tau_tx),  B_n = apo_rx * exp(i 2 pi fd tau_rx)
 //
 // One CTA beamforms a tile of 512 pixels (one per thread) for one frame.  The
-// (channel, wave) pairs are processed in stages of CG x KW; for each pair the
-// tile needs a short window of samples starting at i0 = base_n + base_w, where
-// base_n / base_w are integer lower bounds of the tile's receive / transmit
-// delays (in samples) derived from the tile's bounding box.  The window is
-// staged as interpolation entries {x_i, x_{i+1} - x_i} in FP32 with das_c's
-// validity rule (0 < i < L-1) folded in as zero entries, so a unit costs:
+// (channel, wave) pairs are processed in stages of CG x KW = 32 slots; for each
+// pair the tile needs a short window of samples starting at i0 = base_n + base_w,
+// where base_n / base_w are integer lower bounds of the tile's receive / transmit
+// delays (in samples) derived from the tile's bounding box.
+//
+// A pre-pass (build_entries_kernel) rewrites the channel data, whatever its
+// storage type, as FP32 interpolation entries {x_i, x_{i+1} - x_i} with das_c's
+// validity rule (0 < i < L-1) folded in as zero entries.  A stage's windows are
+// then plain runs of 16-byte (complex) or 8-byte (real) entries that the CTA
+// copies with cp.async into one of two shared-memory buffers while it computes
+// the stage before; no per-sample work is left in the staging.  A unit costs:
 //   s = s_tx_loc + s_rx_loc; j = floor(s); b = s - j; e = slot[j];
 //   v = e.x + b*e.d;  acc += weight * v.
 // Delays relative to the tile bases stay below 80 samples, so j and b keep
@@ -27,6 +32,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -42,8 +48,8 @@ constexpr float kMagic = 8388608.0f;            // 2^23: floor via round-toward-
 constexpr int kMagicBits = 0x4B000000;
 
 struct Params {
-    const void* ch;
-    int64_t L, N, W, F, P;
+    const void* entries;  // [F][W][N][Lp] interpolation entries (float4 complex, float2 real)
+    int64_t L, Lp, N, W, F, P;
     const float* el;
     const float* px;
     const int32_t* tiles;
@@ -246,34 +252,52 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// bytes per stored sample
+// one stored sample (global memory) as float2
 template <int ST, bool CPLX>
-struct StoreInfo {
-    static constexpr int bytes = (ST == USTB_STORE_F32 ? 4 : 2) * (CPLX ? 2 : 1);
-};
-
-// a raw staged sample (shared memory) as float2
-template <int ST, bool CPLX>
-__device__ __forceinline__ float2 raw_sample(const unsigned char* raw, int i) {
+__device__ __forceinline__ float2 load_sample(const void* ch, int64_t i) {
     if constexpr (CPLX) {
-        if constexpr (ST == USTB_STORE_F32) return reinterpret_cast<const float2*>(raw)[i];
-        else if constexpr (ST == USTB_STORE_F16) return __half22float2(reinterpret_cast<const __half2*>(raw)[i]);
-        else return __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(raw)[i]);
+        if constexpr (ST == USTB_STORE_F32) return __ldg(reinterpret_cast<const float2*>(ch) + i);
+        else if constexpr (ST == USTB_STORE_F16) return __half22float2(reinterpret_cast<const __half2*>(ch)[i]);
+        else return __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(ch)[i]);
     } else {
-        if constexpr (ST == USTB_STORE_F32) return make_float2(reinterpret_cast<const float*>(raw)[i], 0.f);
-        else if constexpr (ST == USTB_STORE_F16) return make_float2(__half2float(reinterpret_cast<const __half*>(raw)[i]), 0.f);
-        else return make_float2(__bfloat162float(reinterpret_cast<const __nv_bfloat16*>(raw)[i]), 0.f);
+        if constexpr (ST == USTB_STORE_F32) return make_float2(__ldg(reinterpret_cast<const float*>(ch) + i), 0.f);
+        else if constexpr (ST == USTB_STORE_F16) return make_float2(__half2float(reinterpret_cast<const __half*>(ch)[i]), 0.f);
+        else return make_float2(__bfloat162float(reinterpret_cast<const __nv_bfloat16*>(ch)[i]), 0.f);
     }
 }
 
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+// Interpolation entries of every trace: E[t][i] = {x_i, x_{i+1} - x_i} for
+// 0 < i < L-1 (das_c.cpp:381-383's validity rule), zero elsewhere.  HBM-bound:
+// one pass over the channel data.
+template <int ST, bool CPLX>
+__global__ void __launch_bounds__(256) build_entries_kernel(const void* __restrict__ ch,
+                                                            void* __restrict__ entries, int64_t L, int64_t Lp,
+                                                            int64_t n_traces) {
+    const int64_t total = n_traces * Lp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / Lp, i = e - t * Lp;
+        float2 x0 = make_float2(0.f, 0.f), d = make_float2(0.f, 0.f);
+        if (i >= 1 && i < L - 1) {
+            x0 = load_sample<ST, CPLX>(ch, t * L + i);
+            const float2 x1 = load_sample<ST, CPLX>(ch, t * L + i + 1);
+            d = make_float2(x1.x - x0.x, x1.y - x0.y);
+        }
+        if constexpr (CPLX) reinterpret_cast<float4*>(entries)[e] = make_float4(x0.x, x0.y, d.x, d.y);
+        else reinterpret_cast<float2*>(entries)[e] = make_float2(x0.x, d.x);
+    }
+}
+
+// ---- asynchronous global -> shared copies (cp.async, 16 or 8 bytes per thread) -----
+template <int BYTES>
+__device__ __forceinline__ void cp_async(uint32_t dst, const void* src) {
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-constexpr int kRawSamples = kSlot + 16;  // window + 1 + alignment slack
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Conservative test that channel `n`'s receive window is zero over the whole tile
 // box: every window is 0 for ratio > 1/2 (apodization.m:172-186), and the ratio
@@ -299,31 +323,53 @@ __device__ __forceinline__ bool rx_active(const Params& A, const Box& b, float e
     return !(A.fnx * xd / zx > lim || A.fny * yd / zy > lim);
 }
 
-template <bool CPLX, int ST>
+template <bool CPLX>
 struct CtasPerSm {
     static constexpr int value = 1;  // 512 threads x 128 registers fill the register file
 };
 
+template <bool ORDER_A>
+struct StageShape {
+    static constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
+    static constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
+    static constexpr int NS = CG * KW;           // slots per stage
+};
+constexpr int kStageSlots = 32;
+
+// Shared memory of one CTA: two stage buffers of kStageSlots slots x kSlot entries,
+// then the per-tile tables (their size depends on N and W).
+template <bool CPLX>
+constexpr size_t slot_buffer_bytes() {
+    return (size_t)2 * kStageSlots * kSlot * (CPLX ? 16 : 8);
+}
+
+// Once per CTA, before its first tile: zero the stage buffers, so that units with
+// zero weight, which may read past a window's end, never read uninitialised words.
+template <bool CPLX>
+__device__ __forceinline__ void zero_slots() {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* z = reinterpret_cast<float4*>(smem);
+    for (int i = threadIdx.x; i < (int)(slot_buffer_bytes<CPLX>() / 16); i += blockDim.x)
+        z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+}
+
 // Beamform one tile of one frame (the whole CTA participates).
-template <int MODE, bool CPLX, int ST, bool EPI>
+template <int MODE, bool CPLX, bool EPI>
 __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
-    constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
-    constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
-    constexpr int NS = CG * KW;           // slots per stage
-    constexpr int SB = StoreInfo<ST, CPLX>::bytes;
-    constexpr int SPC = 16 / SB;          // samples per 16-byte chunk
-    constexpr int RAWB = kRawSamples * SB;
-    constexpr int MAXCH = RAWB / 16;
+    constexpr int CG = StageShape<ORDER_A>::CG;
+    constexpr int KW = StageShape<ORDER_A>::KW;
+    constexpr int NS = StageShape<ORDER_A>::NS;
+    static_assert(NS == kStageSlots, "stage buffers hold kStageSlots slots");
     using Entry = typename EntryT<CPLX>::type;
-    static_assert(RAWB % 16 == 0, "raw slot must be a whole number of 16-byte chunks");
+    constexpr int ES = (int)sizeof(Entry);
 
     const int64_t L = A.L, N = A.N, W = A.W, P = A.P;
     extern __shared__ __align__(16) unsigned char smem[];
     Entry* slots = reinterpret_cast<Entry*>(smem);
-    unsigned char* raw_base = smem + (size_t)NS * kSlot * sizeof(Entry);
     const int NG = (int)((N + CG - 1) / CG), NC = (int)((W + KW - 1) / KW);
-    float* base_n = reinterpret_cast<float*>(raw_base + 2 * NS * RAWB);  // integer-valued
+    float* base_n = reinterpret_cast<float*>(smem + slot_buffer_bytes<CPLX>());  // integer-valued
     int* len_n = reinterpret_cast<int*>(base_n + N);
     float* base_w = reinterpret_cast<float*>(len_n + N);
     int* len_w = reinterpret_cast<int*>(base_w + W);
@@ -428,108 +474,46 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
 
     const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
     const float fd_c = A.fd * A.inv_c;
-    const char* chb = reinterpret_cast<const char*>(A.ch);
-    const int64_t TOT = L * N * W * A.F;  // samples in the whole array
-    const int64_t frame_off = f * W * N * L;
+    const int64_t frame_tr = f * W * N;  // first trace of this frame
+    const int Lc = (int)L;               // entries per trace
+    const uint32_t slots_s = (uint32_t)__cvta_generic_to_shared(slots);
+    unsigned bufoff = 0;                 // byte offset of the current stage's buffer
+    auto stage_o = [&](int si) { return stage_list[si] >> 16; };
+    auto stage_i = [&](int si) { return stage_list[si] & 0xFFFF; };
+    auto stage_w0 = [&](int si) { return (ORDER_A ? stage_o(si) : stage_i(si)) * KW; };
+    auto stage_n0 = [&](int si) { return (ORDER_A ? stage_i(si) : stage_o(si)) * CG; };
 
-    // Per-slot staging metadata.  Each warp owns SPW slots of every stage
-    // (slot = warp + NWARPS * r); lane r computes slot r's metadata once and the
-    // warp reads it back with shuffles.
+    // Stage si's windows into buffer `buf`.  Warp v stages slots v and v + 16; its
+    // lanes copy the window [i0, i0 + len) entry by entry with cp.async, and store
+    // zeros for the entries outside the trace.  Slots without work are left as they
+    // are: their units carry zero weight and read finite stale entries.
     constexpr int NWARPS = kTile / 32;
-    constexpr int SPW = (NS + NWARPS - 1) / NWARPS;
-    static_assert(SPW <= 32, "too many slots per warp");
-    struct Meta {
-        int64_t tb;  // global sample index of the trace start
-        int i0, len, act;
-    };
-    auto meta_of = [&](int w0, int n0) {
-        Meta m{0, 0, 0, 0};
-        const int slot = warp + NWARPS * lane;
-        if (lane < SPW && slot < NS) {
-            const int c = slot / KW, k = slot - c * KW;
+    const Entry* ent = reinterpret_cast<const Entry*>(A.entries);
+    auto issue = [&](int si, int buf) {
+        const int w0 = stage_w0(si), n0 = stage_n0(si);
+#pragma unroll
+        for (int r = 0; r < NS / NWARPS; ++r) {
+            const int sl = warp + NWARPS * r;
+            const int c = sl / KW, k = sl - (sl / KW) * KW;
             const int n = n0 + c, w = w0 + k;
-            if (n < N && w < W && act_n[n] && act_w[w]) {
-                m.act = 1;
-                m.len = min(kSlot, len_n[n] + len_w[w] + 3);
-                m.i0 = __float2int_rn(base_n[n] + base_w[w]);
-                m.tb = frame_off + ((int64_t)w * N + n) * L;
-            }
-        }
-        return m;
-    };
-    auto bcast = [&](const Meta& m, int r) {
-        Meta o;
-        o.tb = __shfl_sync(0xffffffffu, m.tb, r);
-        o.i0 = __shfl_sync(0xffffffffu, m.i0, r);
-        o.len = __shfl_sync(0xffffffffu, m.len, r);
-        o.act = __shfl_sync(0xffffffffu, m.act, r);
-        return o;
-    };
-
-    // issue the raw copies of the stage described by `m` into buffer b
-    auto issue = [&](const Meta& m, int b) {
-        unsigned char* rb = raw_base + b * NS * RAWB;
-#pragma unroll
-        for (int r = 0; r < SPW; ++r) {
-            const int slot = warp + NWARPS * r;
-            const Meta q = bcast(m, r);
-            if (slot >= NS || !q.act) continue;
-            const int64_t g0 = q.tb + q.i0;
-            const int64_t ga = g0 & ~(int64_t)(SPC - 1);
-            const int nch = ((int)(g0 - ga) + q.len + 1 + SPC - 1) / SPC;
-            unsigned char* dst = rb + slot * RAWB;
-            for (int ch = lane; ch < nch; ch += 32) {
-                const int64_t cs = ga + (int64_t)ch * SPC;
-                if (cs >= 0 && cs + SPC <= TOT) {
-                    cp_async16(dst + ch * 16, chb + cs * SB);
+            if (!(n < N && w < W && act_n[n] && act_w[w])) continue;
+            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
+            const int i0 = __float2int_rn(base_n[n] + base_w[w]);
+            const Entry* src = ent + (frame_tr + (int64_t)w * N + n) * A.Lp;
+            const uint32_t dst = slots_s + (uint32_t)((buf * NS + sl) * kSlot * ES);
+            for (int j = lane; j < len; j += 32) {
+                const int i = i0 + j;
+                if ((unsigned)i < (unsigned)Lc) {
+                    cp_async<ES>(dst + (uint32_t)(j * ES), src + i);
                 } else {
-#pragma unroll
-                    for (int e = 0; e < SPC; ++e) {
-                        const int64_t idx = cs + e;
-#pragma unroll
-                        for (int by = 0; by < SB; ++by)
-                            dst[ch * 16 + e * SB + by] = (idx >= 0 && idx < TOT) ? (unsigned char)chb[idx * SB + by] : 0;
-                    }
+                    if constexpr (CPLX)
+                        asm volatile("st.shared.v4.f32 [%0], {%1, %1, %1, %1};\n" ::"r"(dst + (uint32_t)(j * ES)), "f"(0.f) : "memory");
+                    else
+                        asm volatile("st.shared.v2.f32 [%0], {%1, %1};\n" ::"r"(dst + (uint32_t)(j * ES)), "f"(0.f) : "memory");
                 }
             }
         }
         cp_async_commit();
-    };
-
-    // raw samples -> interpolation entries {x_i, x_{i+1} - x_i} with das_c's
-    // validity rule (0 < i < L-1); slots without work get zero entries
-    const unsigned Lm2 = (unsigned)(L - 2);
-    auto transform = [&](const Meta& m, int b) {
-        const unsigned char* rb = raw_base + b * NS * RAWB;
-#pragma unroll
-        for (int r = 0; r < SPW; ++r) {
-            const int slot = warp + NWARPS * r;
-            if (slot >= NS) continue;
-            const Meta q = bcast(m, r);
-            Entry* dst = slots + slot * kSlot;
-            if (!q.act) {
-                // units of this slot carry zero weight and read j <= kHalf
-                for (int j = lane; j <= (int)kHalf; j += 32) {
-                    if constexpr (CPLX) dst[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    else dst[j] = make_float2(0.f, 0.f);
-                }
-                continue;
-            }
-            const int off = (int)((q.tb + q.i0) & (int64_t)(SPC - 1));
-            const unsigned char* src = rb + slot * RAWB;
-            for (int j = lane; j < q.len; j += 32) {
-                Entry v;
-                if constexpr (CPLX) v = make_float4(0.f, 0.f, 0.f, 0.f);
-                else v = make_float2(0.f, 0.f);
-                if ((unsigned)(q.i0 + j - 1) < Lm2) {
-                    const float2 x0 = raw_sample<ST, CPLX>(src, off + j);
-                    const float2 x1 = raw_sample<ST, CPLX>(src, off + j + 1);
-                    if constexpr (CPLX) v = make_float4(x0.x, x0.y, x1.x - x0.x, x1.y - x0.y);
-                    else v = make_float2(x0.x, x1.x - x0.x);
-                }
-                dst[j] = v;
-            }
-        }
     };
 
     // per-thread geometry
@@ -599,7 +583,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
     auto interp = [&](int c, int k, float s) -> float2 {
         const float t = __fadd_rz(s, kMagic);
         const float b = s - (t - kMagic);
-        const unsigned addr = (unsigned)__float_as_int(t) * (unsigned)sizeof(Entry) + slot0 +
+        const unsigned addr = (unsigned)__float_as_int(t) * (unsigned)sizeof(Entry) + (slot0 + bufoff) +
                               (unsigned)((c * KW + k) * kSlot * (int)sizeof(Entry));
         if constexpr (CPLX) {
             float4 e;
@@ -619,31 +603,16 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
         else reinterpret_cast<float*>(A.cube)[o] = y.x;
     };
 
-    // pipeline over the tile's active stages: stage si+1's copies are in flight
-    // while stage si is transformed and computed
-    int buf = 0;
-    auto stage_o = [&](int si) { return stage_list[si] >> 16; };
-    auto stage_i = [&](int si) { return stage_list[si] & 0xFFFF; };
-    auto stage_w0 = [&](int si) { return (ORDER_A ? stage_o(si) : stage_i(si)) * KW; };
-    auto stage_n0 = [&](int si) { return (ORDER_A ? stage_i(si) : stage_o(si)) * CG; };
-    Meta m_cur{0, 0, 0, 0}, m_nxt{0, 0, 0, 0};
-    if (nstages > 0) {
-        m_cur = meta_of(stage_w0(0), stage_n0(0));
-        issue(m_cur, 0);
-    }
-    auto run_stage = [&](int si) {
-        if (si + 1 < nstages) {
-            m_nxt = meta_of(stage_w0(si + 1), stage_n0(si + 1));
-            issue(m_nxt, buf ^ 1);
-        } else {
-            cp_async_commit();  // keep one group per stage
-        }
-        cp_async_wait_prev();
-        __syncthreads();  // raw(si) visible everywhere; previous stage's entries consumed
-        transform(m_cur, buf);
+    // Double-buffered pipeline over the tile's active stages: stage si + 1's windows
+    // are copied while stage si is computed.  One barrier per stage: it makes stage
+    // si's entries visible to every warp and frees the other buffer (read by stage
+    // si - 1) for stage si + 1's copies.
+    if (nstages > 0) issue(0, 0);
+    auto begin_stage = [&](int si) {
+        cp_async_wait_all();
         __syncthreads();
-        m_cur = m_nxt;
-        buf ^= 1;
+        if (si + 1 < nstages) issue(si + 1, (si + 1) & 1);
+        bufoff = (unsigned)((si & 1) * NS * kSlot * ES);
     };
     const float2 zero2 = make_float2(0.f, 0.f);
 
@@ -681,8 +650,8 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
                 for (int k = 0; k < KW; ++k) accr[k] = acci[k] = 0.f;
             }
             const int n0 = stage_n0(si);
-            run_stage(si);
             setup_rx(n0);
+            begin_stage(si);
             const int kw = min(KW, (int)W - cur * KW);
             auto units = [&](auto full) {
 #pragma unroll
@@ -750,8 +719,8 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
                 for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
             }
             const int w0 = stage_w0(si), n0 = og * CG;
-            run_stage(si);
             setup_tx(w0);
+            begin_stage(si);
 #pragma unroll
             for (int c = 0; c < CG; ++c) {
 #pragma unroll
@@ -786,14 +755,14 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
             }
         }
     }
-    cp_async_commit();
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();  // the buffers and per-tile tables are reused by the next tile
 }
 
 // One launch per request: grid = (tiles, frames).
-template <int MODE, bool CPLX, int ST, bool EPI>
-__global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX, ST>::value)) das_fast_kernel(const Params A) {
-    das_tile<MODE, CPLX, ST, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
+template <int MODE, bool CPLX, bool EPI>
+__global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX>::value)) das_fast_kernel(const Params A) {
+    zero_slots<CPLX>();
+    das_tile<MODE, CPLX, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
 }
 
 // Persistent form: one CTA per SM pulls (request, frame, tile) work items from a
@@ -807,9 +776,10 @@ struct BatchParams {
     unsigned long long* counter;        // queue head (device scratch, zeroed per launch)
 };
 
-template <int MODE, bool CPLX, int ST, bool EPI>
+template <int MODE, bool CPLX, bool EPI>
 __global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_constant__ BatchParams B) {
     __shared__ long long s_item;
+    zero_slots<CPLX>();
     const int64_t total = B.first_item[B.n];
     for (;;) {
         if (threadIdx.x == 0) s_item = (long long)atomicAdd(B.counter, 1ull);
@@ -821,33 +791,29 @@ __global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_con
         while (r + 1 < B.n && B.first_item[r + 1] <= item) ++r;
         const Params& A = B.req[r];
         const int64_t local = item - B.first_item[r];
-        das_tile<MODE, CPLX, ST, EPI>(A, (int)(local % A.n_tiles), local / A.n_tiles);
-        __syncthreads();  // shared memory is reused by the next item
+        das_tile<MODE, CPLX, EPI>(A, (int)(local % A.n_tiles), local / A.n_tiles);
     }
 }
 
-template <int MODE, bool CPLX, int ST, bool EPI>
+template <int MODE, bool CPLX, bool EPI>
 size_t smem_bytes(int64_t N, int64_t W) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
-    constexpr int NS = ORDER_A ? 2 * 16 : 8 * 4;
-    const size_t entries = (size_t)NS * kSlot * (CPLX ? 16 : 8);
-    const size_t raw = 2 * (size_t)NS * kRawSamples * StoreInfo<ST, CPLX>::bytes;
-    const int CG = ORDER_A ? 2 : 8, KW = ORDER_A ? 16 : 4;
+    constexpr int CG = StageShape<ORDER_A>::CG, KW = StageShape<ORDER_A>::KW;
     const size_t NG = (size_t)((N + CG - 1) / CG), NC = (size_t)((W + KW - 1) / KW);
     const size_t hdr = 8 * (size_t)(N + W) + 4 * NG * NC + (size_t)(N + W) + NG + NC;
-    return entries + raw + ((hdr + 15) & ~size_t(15));
+    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15));
 }
 
-template <int MODE, bool CPLX, int ST, bool EPI>
+template <int MODE, bool CPLX, bool EPI>
 int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
-    const size_t smem = smem_bytes<MODE, CPLX, ST, EPI>(A.N, A.W);
+    const size_t smem = smem_bytes<MODE, CPLX, EPI>(A.N, A.W);
     int dev = 0, optin = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE,
                  "%lld channels / %lld waves need %zu bytes of shared memory per tile (limit %d)",
                  (long long)A.N, (long long)A.W, smem, optin);
-    auto kern = das_fast_kernel<MODE, CPLX, ST, EPI>;
+    auto kern = das_fast_kernel<MODE, CPLX, EPI>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)n_tiles, (unsigned)F);
     kern<<<grid, kTile, smem, s>>>(A);
@@ -855,7 +821,7 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
     return USTB_OK;
 }
 
-template <int MODE, bool CPLX, int ST, bool EPI>
+template <int MODE, bool CPLX, bool EPI>
 int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long long* counter, cudaStream_t s) {
     BatchParams B;
     B.n = n;
@@ -865,7 +831,7 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     for (int i = 0; i < n; ++i) {
         B.req[i] = reqs[i];
         B.first_item[i + 1] = B.first_item[i] + reqs[i].n_tiles * frames[i];
-        smem = std::max(smem, smem_bytes<MODE, CPLX, ST, EPI>(reqs[i].N, reqs[i].W));
+        smem = std::max(smem, smem_bytes<MODE, CPLX, EPI>(reqs[i].N, reqs[i].W));
     }
     if (B.first_item[n] == 0) return USTB_OK;
     int dev = 0, optin = 0, sms = 0;
@@ -874,7 +840,7 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "a request needs %zu bytes of shared memory per tile (limit %d)",
                  smem, optin);
-    auto kern = das_fast_persistent<MODE, CPLX, ST, EPI>;
+    auto kern = das_fast_persistent<MODE, CPLX, EPI>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     USTB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
     const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], (int64_t)sms);
@@ -883,31 +849,89 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     return USTB_OK;
 }
 
-template <bool CPLX, int ST>
+template <bool CPLX>
 int dispatch_batch(int dim, int epi, const Params* reqs, const int64_t* frames, int n,
                    unsigned long long* counter, cudaStream_t s) {
     switch (dim) {
-        case USTB_DIM_NONE: return launch_batch<USTB_DIM_NONE, CPLX, ST, false>(reqs, frames, n, counter, s);
-        case USTB_DIM_RECEIVE: return launch_batch<USTB_DIM_RECEIVE, CPLX, ST, false>(reqs, frames, n, counter, s);
+        case USTB_DIM_NONE: return launch_batch<USTB_DIM_NONE, CPLX, false>(reqs, frames, n, counter, s);
+        case USTB_DIM_RECEIVE: return launch_batch<USTB_DIM_RECEIVE, CPLX, false>(reqs, frames, n, counter, s);
         case USTB_DIM_TRANSMIT:
             if constexpr (CPLX)
-                if (epi) return launch_batch<USTB_DIM_TRANSMIT, CPLX, ST, true>(reqs, frames, n, counter, s);
-            return launch_batch<USTB_DIM_TRANSMIT, CPLX, ST, false>(reqs, frames, n, counter, s);
-        default: return launch_batch<USTB_DIM_BOTH, CPLX, ST, false>(reqs, frames, n, counter, s);
+                if (epi) return launch_batch<USTB_DIM_TRANSMIT, CPLX, true>(reqs, frames, n, counter, s);
+            return launch_batch<USTB_DIM_TRANSMIT, CPLX, false>(reqs, frames, n, counter, s);
+        default: return launch_batch<USTB_DIM_BOTH, CPLX, false>(reqs, frames, n, counter, s);
     }
 }
 
-template <bool CPLX, int ST>
+template <bool CPLX>
 int dispatch_mode(int dim, int epi, const Params& A, int64_t nt, int64_t F, cudaStream_t s) {
     switch (dim) {
-        case USTB_DIM_NONE: return launch<USTB_DIM_NONE, CPLX, ST, false>(A, nt, F, s);
-        case USTB_DIM_RECEIVE: return launch<USTB_DIM_RECEIVE, CPLX, ST, false>(A, nt, F, s);
+        case USTB_DIM_NONE: return launch<USTB_DIM_NONE, CPLX, false>(A, nt, F, s);
+        case USTB_DIM_RECEIVE: return launch<USTB_DIM_RECEIVE, CPLX, false>(A, nt, F, s);
         case USTB_DIM_TRANSMIT:
             if constexpr (CPLX)
-                if (epi) return launch<USTB_DIM_TRANSMIT, CPLX, ST, true>(A, nt, F, s);
-            return launch<USTB_DIM_TRANSMIT, CPLX, ST, false>(A, nt, F, s);
-        default: return launch<USTB_DIM_BOTH, CPLX, ST, false>(A, nt, F, s);
+                if (epi) return launch<USTB_DIM_TRANSMIT, CPLX, true>(A, nt, F, s);
+            return launch<USTB_DIM_TRANSMIT, CPLX, false>(A, nt, F, s);
+        default: return launch<USTB_DIM_BOTH, CPLX, false>(A, nt, F, s);
     }
+}
+
+// ---- entries scratch ---------------------------------------------------------
+int64_t entry_bytes(int64_t L, int64_t N, int64_t W, int64_t F, bool cplx) {
+    return L * N * W * F * (cplx ? 16 : 8);
+}
+
+// A stream-ordered memory pool owned by the library (one per device) that keeps
+// freed entry arrays for the next call instead of returning them to the driver.
+cudaMemPool_t entry_pool(int dev) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        pools[dev] = p;
+    }
+    return pools[dev];
+}
+
+// Allocate (stream-ordered, from the library pool) and fill one request's entries.
+int build_entries(const void* ch, int32_t storage, bool cplx, int64_t L, int64_t N, int64_t W, int64_t F,
+                  void** out, cudaStream_t s) {
+    *out = nullptr;
+    const int64_t bytes = entry_bytes(L, N, W, F, cplx);
+    if (bytes == 0) return USTB_OK;
+    int dev = 0, sms = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaMemPool_t pool = entry_pool(dev);
+    USTB_REQUIRE(pool, USTB_E_CUDA, "could not create the entry memory pool on device %d", dev);
+    const cudaError_t e = cudaMallocFromPoolAsync(out, (size_t)bytes, pool, s);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        *out = nullptr;
+        ustb::set_error("%lld bytes of interpolation entries: %s", (long long)bytes, cudaGetErrorString(e));
+        return USTB_E_OOM;
+    }
+    const int64_t traces = N * W * F, total = traces * L;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16);
+    switch (storage * 2 + (cplx ? 1 : 0)) {
+        case USTB_STORE_F32 * 2 + 1: build_entries_kernel<USTB_STORE_F32, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+        case USTB_STORE_F16 * 2 + 1: build_entries_kernel<USTB_STORE_F16, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+        case USTB_STORE_BF16 * 2 + 1: build_entries_kernel<USTB_STORE_BF16, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+        case USTB_STORE_F32 * 2: build_entries_kernel<USTB_STORE_F32, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+        case USTB_STORE_F16 * 2: build_entries_kernel<USTB_STORE_F16, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+        default: build_entries_kernel<USTB_STORE_BF16, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+    }
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
 }
 
 }  // namespace
@@ -950,8 +974,8 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
         empty = true;
         return USTB_OK;
     }
-    A.ch = ch;
-    A.L = L; A.N = N; A.W = W; A.F = F; A.P = P;
+    A.entries = nullptr;  // built by the caller of make_params
+    A.L = L; A.Lp = L; A.N = N; A.W = W; A.F = F; A.P = P;
     A.el = g->element_xyz;
     A.px = g->pixel_xyz;
     A.tiles = g->tile_pixels;
@@ -997,19 +1021,17 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     bool empty = false;
     int rc = make_params(ch, storage, is_complex, L, N, W, F, g, dimension, epilogue, out, flags, s, A, empty);
     if (rc || empty) return rc;
+    void* ent = nullptr;
+    rc = build_entries(ch, storage, is_complex != 0, L, N, W, F, &ent, s);
+    if (rc) return rc;
+    A.entries = ent;
     const int64_t nt = g->n_tiles;
-    if (is_complex) {
-        switch (storage) {
-            case USTB_STORE_F32: return dispatch_mode<true, USTB_STORE_F32>(dimension, epilogue, A, nt, F, s);
-            case USTB_STORE_F16: return dispatch_mode<true, USTB_STORE_F16>(dimension, epilogue, A, nt, F, s);
-            default: return dispatch_mode<true, USTB_STORE_BF16>(dimension, epilogue, A, nt, F, s);
-        }
-    }
-    switch (storage) {
-        case USTB_STORE_F32: return dispatch_mode<false, USTB_STORE_F32>(dimension, 0, A, nt, F, s);
-        case USTB_STORE_F16: return dispatch_mode<false, USTB_STORE_F16>(dimension, 0, A, nt, F, s);
-        default: return dispatch_mode<false, USTB_STORE_BF16>(dimension, 0, A, nt, F, s);
-    }
+    rc = is_complex ? dispatch_mode<true>(dimension, epilogue, A, nt, F, s)
+                    : dispatch_mode<false>(dimension, 0, A, nt, F, s);
+    const cudaError_t fe = cudaFreeAsync(ent, s);
+    if (rc) return rc;
+    USTB_CUDA(fe);
+    return USTB_OK;
 }
 
 extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream) {
@@ -1036,7 +1058,25 @@ extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint
             return rc;
         }
         frames[i] = q.F;
-        if (!empty) key[i] = ((q.dimension * 2 + q.is_complex) * 3 + q.storage) * 2 + (q.epilogue ? 1 : 0);
+        if (!empty) key[i] = (q.dimension * 2 + q.is_complex) * 2 + (q.epilogue ? 1 : 0);
+    }
+    // every request's entry array, freed (stream-ordered) after the launches
+    std::vector<void*> ents;
+    auto release = [&]() {
+        for (void* e : ents) (void)cudaFreeAsync(e, s);
+        ents.clear();
+    };
+    for (int i = 0; i < n; ++i) {
+        if (key[i] < 0) continue;
+        const ustb_das_request& q = reqs[i];
+        void* ent = nullptr;
+        const int rc = build_entries(q.ch, q.storage, q.is_complex != 0, q.L, q.N, q.W, q.F, &ent, s);
+        if (rc) {
+            release();
+            return rc;
+        }
+        ents.push_back(ent);
+        P[i].entries = ent;
     }
     int group = 0;
     std::vector<bool> done(n, false);
@@ -1055,23 +1095,20 @@ extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint
             const int cnt = (int)std::min<size_t>(kMaxBatch, gp.size() - off);
             unsigned long long* counter = reinterpret_cast<unsigned long long*>(scratch + 1 + group);
             ++group;
-            USTB_REQUIRE(group <= n, USTB_E_ARG, "scratch holds n + 1 words");
-            int rc;
-            if (q.is_complex) {
-                switch (q.storage) {
-                    case USTB_STORE_F32: rc = dispatch_batch<true, USTB_STORE_F32>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                    case USTB_STORE_F16: rc = dispatch_batch<true, USTB_STORE_F16>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                    default: rc = dispatch_batch<true, USTB_STORE_BF16>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                }
-            } else {
-                switch (q.storage) {
-                    case USTB_STORE_F32: rc = dispatch_batch<false, USTB_STORE_F32>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                    case USTB_STORE_F16: rc = dispatch_batch<false, USTB_STORE_F16>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                    default: rc = dispatch_batch<false, USTB_STORE_BF16>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s); break;
-                }
+            if (group > n) {
+                release();
+                ustb::set_error("scratch holds n + 1 words");
+                return USTB_E_ARG;
             }
-            if (rc) return rc;
+            const int rc = q.is_complex
+                               ? dispatch_batch<true>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s)
+                               : dispatch_batch<false>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s);
+            if (rc) {
+                release();
+                return rc;
+            }
         }
     }
+    release();
     return USTB_OK;
 }

@@ -362,6 +362,12 @@ class FastGeometry:
         return self.P * self.N * self.W * F
 
 
+def entry_bytes(L: int, N: int, W: int, F: int, is_complex: bool) -> int:
+    """Bytes of the FP32 interpolation entries ``ustb_das_fast`` builds for one request
+    (16 per complex sample, 8 per real one)."""
+    return L * N * W * F * (16 if is_complex else 8)
+
+
 def convert_channels(src: torch.Tensor, precision: Precision, scale: float = 1.0) -> torch.Tensor:
     """Channel data -> device storage type through ``ustb_convert_channels``.
 

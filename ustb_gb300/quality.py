@@ -93,8 +93,9 @@ def isolated_points(points: np.ndarray, scan: LinearScan, cysts: Sequence[Tuple[
 
 
 def compare(img: np.ndarray, ref: np.ndarray, scan: LinearScan, cysts: Sequence[Tuple[float, float, float]],
-            points: np.ndarray, max_points: int = 10) -> Dict[str, object]:
-    """Relative L2 error, per-cyst contrast and per-point FWHM of ``img`` against ``ref``."""
+            points: np.ndarray, max_points: int = 10, min_separation: float = 2e-3) -> Dict[str, object]:
+    """Relative L2 error, per-cyst contrast and per-point FWHM of ``img`` against ``ref``
+    (point targets with no neighbour within ``min_separation``)."""
     img = np.asarray(img).reshape(-1)
     ref = np.asarray(ref).reshape(-1)
     out: Dict[str, object] = {"rel_l2": float(np.linalg.norm(img - ref) / np.linalg.norm(ref))}
@@ -105,7 +106,7 @@ def compare(img: np.ndarray, ref: np.ndarray, scan: LinearScan, cysts: Sequence[
     out["contrast_db"] = cr
     out["max_contrast_diff_db"] = max((abs(a - b) for a, b in cr), default=0.0)
     fw: List[Tuple[float, float]] = []
-    for i in isolated_points(points, scan, cysts)[:max_points]:
+    for i in isolated_points(points, scan, cysts, min_separation)[:max_points]:
         x, _, z = points[i]
         fw.append((lateral_fwhm(img, scan, x, z), lateral_fwhm(ref, scan, x, z)))
     fw = [(a, b) for a, b in fw if np.isfinite(a) and np.isfinite(b)]

@@ -76,13 +76,16 @@ class Server:
 
     # -- requests ----------------------------------------------------------------
     def _bytes(self, job: Job) -> int:
+        """Device bytes a job holds while in flight: channel data, outputs and the
+        interpolation entries its launch builds."""
         g = self.plans[job.key]
         out = g.P * job.F * (8 if job.is_complex else 4)
         if job.dimension in (0, 2):
             out *= g.N
         if job.dimension in (0, 1):
             out *= g.W
-        return int(job.ch.numel() * job.ch.element_size() + out)
+        ent = fast.entry_bytes(job.L, g.N, g.W, job.F, job.is_complex)
+        return int(job.ch.numel() * job.ch.element_size() + out + ent)
 
     def submit(self, job: Job, now: Optional[float] = None) -> Job:
         if job.key not in self.plans:
