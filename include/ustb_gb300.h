@@ -267,6 +267,24 @@ typedef struct {
 int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream);
 
 /*
+ * Device bytes that ustb_das_fast_batch_ws needs as workspace for this batch:
+ * the FP32 interpolation entries of every request, each on a 256-byte boundary.
+ * No reference counterpart (the reference keeps no device working set).
+ */
+int64_t ustb_das_fast_workspace_bytes(const ustb_das_request* reqs, int32_t n);
+
+/*
+ * ustb_das_fast_batch with the entry arrays carved from a caller-owned device
+ * workspace (256-byte aligned, at least ustb_das_fast_workspace_bytes bytes)
+ * instead of the library's memory pool, so the call performs no stream-ordered
+ * allocation: for callers that account device memory themselves (a serving
+ * budget) or that record the launch into a CUDA graph.  Same results as
+ * ustb_das_fast_batch; USTB_E_SHAPE when the workspace is too small.
+ */
+int ustb_das_fast_batch_ws(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
+                           int64_t workspace_bytes, void* stream);
+
+/*
  * Convert channel data to a device storage type: count scalars from `src`
  * (USTB_SRC_*) times `scale` into `dst` (USTB_STORE_*), e.g. int16 I/Q scanner
  * samples or complex64 into half.  Device pointers; stream-ordered.

@@ -1,0 +1,46 @@
+"""Tile-plan tuning: candidates, block planning and the JSON cache (CPU)."""
+import json
+
+import numpy as np
+import pytest
+
+from ustb_gb300 import autotune, fast
+from ustb_gb300.uff import LinearScan, LinearScan3D
+
+
+def test_plan_tiles_with_a_given_block_covers_every_pixel_once():
+    scan = LinearScan(np.linspace(-5e-3, 5e-3, 40), np.linspace(10e-3, 20e-3, 100))
+    tiles = fast.plan_tiles(scan, 20e6, 1540.0, block=(64, 8, 1))
+    got = np.sort(tiles[tiles >= 0])
+    assert np.array_equal(got, np.arange(scan.N_pixels))
+    # blocks are at most 64 deep and 8 wide: every tile's pixels span <= 64 z rows
+    for row in tiles:
+        p = row[row >= 0]
+        iz, ix = p % 100, p // 100
+        assert iz.max() - iz.min() < 64 and ix.max() - ix.min() < 8
+
+
+def test_plan_tiles_rejects_oversized_blocks():
+    scan = LinearScan(np.linspace(-5e-3, 5e-3, 40), np.linspace(10e-3, 20e-3, 100))
+    with pytest.raises(ValueError):
+        fast.plan_tiles(scan, 20e6, 1540.0, block=(32, 32, 1))
+
+
+def test_candidates_2d_and_3d():
+    s2 = LinearScan(np.linspace(-1e-2, 1e-2, 256), np.linspace(5e-3, 5e-2, 512))
+    c2 = autotune.candidates(s2)
+    assert c2[0].block is None and {c.order for c in c2} == {"cost", "scan"}
+    assert all(np.prod(c.block) == fast.TILE for c in c2 if c.block is not None)
+    s3 = LinearScan3D(np.linspace(-1e-2, 1e-2, 64), np.linspace(5e-3, 4e-2, 128), np.linspace(-1e-2, 1e-2, 64))
+    c3 = autotune.candidates(s3)
+    assert any(c.block is not None and c.block[2] > 1 for c in c3)
+
+
+def test_cache_roundtrip_skips_the_search(tmp_path, monkeypatch):
+    monkeypatch.setenv("USTB_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
+    autotune._store("k", autotune.Choice((16, 32, 1), "scan", 1.5))
+    calls = []
+    got = autotune.tune(lambda b, o: calls.append((b, o)), lambda g: None, "k")
+    assert got.block == (16, 32, 1) and got.order == "scan" and got.ms == 1.5 and not calls
+    data = json.load(open(tmp_path / "t.json"))
+    assert data["k"]["order"] == "scan"

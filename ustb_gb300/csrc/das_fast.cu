@@ -902,15 +902,35 @@ cudaMemPool_t entry_pool(int dev) {
     return pools[dev];
 }
 
+// Fill one request's entry array `dst` (entry_bytes(...) bytes of device memory).
+int fill_entries(const void* ch, int32_t storage, bool cplx, int64_t L, int64_t N, int64_t W, int64_t F,
+                 void* dst, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t traces = N * W * F, total = traces * L;
+    if (total == 0) return USTB_OK;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16);
+    switch (storage * 2 + (cplx ? 1 : 0)) {
+        case USTB_STORE_F32 * 2 + 1: build_entries_kernel<USTB_STORE_F32, true><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+        case USTB_STORE_F16 * 2 + 1: build_entries_kernel<USTB_STORE_F16, true><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+        case USTB_STORE_BF16 * 2 + 1: build_entries_kernel<USTB_STORE_BF16, true><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+        case USTB_STORE_F32 * 2: build_entries_kernel<USTB_STORE_F32, false><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+        case USTB_STORE_F16 * 2: build_entries_kernel<USTB_STORE_F16, false><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+        default: build_entries_kernel<USTB_STORE_BF16, false><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
+    }
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
 // Allocate (stream-ordered, from the library pool) and fill one request's entries.
 int build_entries(const void* ch, int32_t storage, bool cplx, int64_t L, int64_t N, int64_t W, int64_t F,
                   void** out, cudaStream_t s) {
     *out = nullptr;
     const int64_t bytes = entry_bytes(L, N, W, F, cplx);
     if (bytes == 0) return USTB_OK;
-    int dev = 0, sms = 0;
+    int dev = 0;
     USTB_CUDA(cudaGetDevice(&dev));
-    USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     cudaMemPool_t pool = entry_pool(dev);
     USTB_REQUIRE(pool, USTB_E_CUDA, "could not create the entry memory pool on device %d", dev);
     const cudaError_t e = cudaMallocFromPoolAsync(out, (size_t)bytes, pool, s);
@@ -920,18 +940,19 @@ int build_entries(const void* ch, int32_t storage, bool cplx, int64_t L, int64_t
         ustb::set_error("%lld bytes of interpolation entries: %s", (long long)bytes, cudaGetErrorString(e));
         return USTB_E_OOM;
     }
-    const int64_t traces = N * W * F, total = traces * L;
-    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16);
-    switch (storage * 2 + (cplx ? 1 : 0)) {
-        case USTB_STORE_F32 * 2 + 1: build_entries_kernel<USTB_STORE_F32, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
-        case USTB_STORE_F16 * 2 + 1: build_entries_kernel<USTB_STORE_F16, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
-        case USTB_STORE_BF16 * 2 + 1: build_entries_kernel<USTB_STORE_BF16, true><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
-        case USTB_STORE_F32 * 2: build_entries_kernel<USTB_STORE_F32, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
-        case USTB_STORE_F16 * 2: build_entries_kernel<USTB_STORE_F16, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
-        default: build_entries_kernel<USTB_STORE_BF16, false><<<grid, 256, 0, s>>>(ch, *out, L, L, traces); break;
+    return fill_entries(ch, storage, cplx, L, N, W, F, *out, s);
+}
+
+// Bytes of a caller workspace that holds the entries of every request of a batch
+// (each request's array starts on a 256-byte boundary).
+int64_t batch_workspace_bytes(const ustb_das_request* reqs, int32_t n) {
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        const ustb_das_request& q = reqs[i];
+        if (q.L <= 0 || q.N <= 0 || q.W <= 0 || q.F <= 0) continue;
+        total += (entry_bytes(q.L, q.N, q.W, q.F, q.is_complex != 0) + 255) & ~int64_t(255);
     }
-    USTB_CUDA(cudaGetLastError());
-    return USTB_OK;
+    return total;
 }
 
 }  // namespace
@@ -1034,7 +1055,8 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     return USTB_OK;
 }
 
-extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream) {
+static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
+                               int64_t workspace_bytes, void* stream) {
     ustb::clear_error();
     USTB_REQUIRE(n >= 0 && (n == 0 || reqs), USTB_E_ARG, "bad request array");
     USTB_REQUIRE(scratch, USTB_E_ARG, "scratch pointer is NULL");
@@ -1060,22 +1082,37 @@ extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint
         frames[i] = q.F;
         if (!empty) key[i] = (q.dimension * 2 + q.is_complex) * 2 + (q.epilogue ? 1 : 0);
     }
-    // every request's entry array, freed (stream-ordered) after the launches
+    // every request's entry array: carved from the caller's workspace, or allocated
+    // from the library pool and freed (stream-ordered) after the launches
     std::vector<void*> ents;
     auto release = [&]() {
         for (void* e : ents) (void)cudaFreeAsync(e, s);
         ents.clear();
     };
+    if (workspace) {
+        const int64_t need = batch_workspace_bytes(reqs, n);
+        USTB_REQUIRE(need <= workspace_bytes, USTB_E_SHAPE, "the workspace holds %lld bytes, the batch needs %lld",
+                     (long long)workspace_bytes, (long long)need);
+        USTB_REQUIRE(((uintptr_t)workspace & 255) == 0, USTB_E_ARG, "the workspace must be 256-byte aligned");
+    }
+    int64_t ws_off = 0;
     for (int i = 0; i < n; ++i) {
         if (key[i] < 0) continue;
         const ustb_das_request& q = reqs[i];
         void* ent = nullptr;
-        const int rc = build_entries(q.ch, q.storage, q.is_complex != 0, q.L, q.N, q.W, q.F, &ent, s);
+        int rc;
+        if (workspace) {
+            ent = static_cast<char*>(workspace) + ws_off;
+            ws_off += (entry_bytes(q.L, q.N, q.W, q.F, q.is_complex != 0) + 255) & ~int64_t(255);
+            rc = fill_entries(q.ch, q.storage, q.is_complex != 0, q.L, q.N, q.W, q.F, ent, s);
+        } else {
+            rc = build_entries(q.ch, q.storage, q.is_complex != 0, q.L, q.N, q.W, q.F, &ent, s);
+            if (!rc) ents.push_back(ent);
+        }
         if (rc) {
             release();
             return rc;
         }
-        ents.push_back(ent);
         P[i].entries = ent;
     }
     int group = 0;
@@ -1111,4 +1148,23 @@ extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint
     }
     release();
     return USTB_OK;
+}
+
+extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream) {
+    return das_fast_batch_impl(reqs, n, scratch, nullptr, 0, stream);
+}
+
+extern "C" int64_t ustb_das_fast_workspace_bytes(const ustb_das_request* reqs, int32_t n) {
+    if (n <= 0 || !reqs) return 0;
+    return batch_workspace_bytes(reqs, n);
+}
+
+extern "C" int ustb_das_fast_batch_ws(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
+                                      int64_t workspace_bytes, void* stream) {
+    if (!workspace) {
+        ustb::clear_error();
+        ustb::set_error("workspace pointer is NULL (ustb_das_fast_batch allocates its own)");
+        return USTB_E_ARG;
+    }
+    return das_fast_batch_impl(reqs, n, scratch, workspace, workspace_bytes, stream);
 }

@@ -149,7 +149,9 @@ class DAS:
             raise ValueError("The modulation frequency > 0 but the input data is real. Check inputs.")
         return ch
 
-    def fast_geometry(self, dev) -> "fast.FastGeometry":
+    def fast_geometry(self, dev, tile_block=None, tile_order: str = "cost") -> "fast.FastGeometry":
+        """Device geometry for the fast engine; ``tile_block`` / ``tile_order`` as chosen
+        by ``autotune`` (default: the planner's own)."""
         from . import fast
 
         cd = self.channel_data
@@ -159,7 +161,8 @@ class DAS:
                                  float(cd.initial_time), fd, float(cd.sound_speed), dev,
                                  self.receive_apodization, self.transmit_apodization,
                                  self.lens_delay, self.spherical_transmit_delay_model,
-                                 self.pw_margin, self.blending_power, pixel_phase=ph)
+                                 self.pw_margin, self.blending_power, pixel_phase=ph,
+                                 tile_block=tile_block, tile_order=tile_order)
 
     def _go_fast(self) -> BeamformedData:
         from . import fast

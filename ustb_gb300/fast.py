@@ -120,12 +120,15 @@ def _block_dims(spacing, shape, ndim_target=TILE):
         dims[bi] *= 2
 
 
-def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SPAN_LIMIT) -> np.ndarray:
+def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SPAN_LIMIT,
+               block: Optional[Sequence[int]] = None) -> np.ndarray:
     """Group pixel indices into tiles of 512 lanes (-1 = idle lane).
 
     A tile's receive and transmit delay spans are bounded by its bounding-box
     diagonal; tiles are shrunk until that diagonal is below
-    ``span_limit`` samples of one-way travel."""
+    ``span_limit`` samples of one-way travel.  ``block``: the tile's pixel block
+    along the scan's axes (depth, lateral, elevation), product <= 512; default:
+    the block whose physical extents are the most even."""
     xyz = scan.xyz
     P = scan.N_pixels
     limit = span_limit * sound_speed / fs
@@ -150,7 +153,12 @@ def plan_tiles(scan: Scan, fs: float, sound_speed: float, span_limit: float = SP
             _split_blocks(order[i:i + TILE], xyz, limit, blocks)
         return _pack(blocks)
     idx = np.arange(P).reshape(shape, order="F")
-    bd = _block_dims(spacing, shape)
+    if block is None:
+        bd = _block_dims(spacing, shape)
+    else:
+        bd = [max(1, min(int(b), n)) for b, n in zip(tuple(block) + (1,) * (3 - len(block)), shape)]
+        if int(np.prod(bd)) > TILE:
+            raise ValueError(f"tile block {tuple(block)} holds more than {TILE} pixels")
     blocks = []
     for i in range(0, shape[0], bd[0]):
         for j in range(0, shape[1], bd[1]):
@@ -246,7 +254,8 @@ class FastGeometry:
                  tx_apodization: Optional[Apodization] = None, lens_delay: float = 0.0,
                  model: STDM = STDM.hybrid, pw_margin: float = 1e-3, blending_power: float = 0.5,
                  pixel_phase: Optional[np.ndarray] = None, cf_threshold: float = 0.16,
-                 tiles: Optional[np.ndarray] = None):
+                 tiles: Optional[np.ndarray] = None, tile_block: Optional[Sequence[int]] = None,
+                 tile_order: str = "cost"):
         dev = torch.device(device)
         rx = rx_apodization or Apodization()
         tx = tx_apodization or Apodization()
@@ -256,9 +265,10 @@ class FastGeometry:
         f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
         self.d_el = f32(probe.xyz)
         self.d_px = f32(scan.xyz)
+        self.tile_block, self.tile_order = tile_block, tile_order
         if tiles is None:
-            self.tiles = plan_tiles(scan, fs, sound_speed)
-            if rx.origin is None and not isinstance(scan, SectorScan):
+            self.tiles = plan_tiles(scan, fs, sound_speed, block=tile_block)
+            if tile_order == "cost" and rx.origin is None and not isinstance(scan, SectorScan):
                 self.tiles = order_by_cost(self.tiles, scan.xyz, probe.xyz, rx)
         else:
             self.tiles = np.asarray(tiles, np.int32)
@@ -473,9 +483,22 @@ class Request:
         return q
 
 
-def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] = None, stream=None):
+def workspace_bytes(requests: Sequence[Request]) -> int:
+    """Device bytes ``das_fast_batch(..., workspace=...)`` needs for these requests."""
+    if not requests:
+        return 0
+    arr = (CRequest * len(requests))(*[r.c_struct() for r in requests])
+    return int(_lib.lib().ustb_das_fast_workspace_bytes(ctypes.addressof(arr), len(requests)))
+
+
+def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] = None, stream=None,
+                   workspace: Optional[torch.Tensor] = None):
     """Beamform a batch of requests with the persistent work-queue kernel
-    (``ustb_das_fast_batch``).  Returns the int64 scratch tensor (word 0 = flags)."""
+    (``ustb_das_fast_batch``).  Returns the int64 scratch tensor (word 0 = flags).
+
+    ``workspace``: optional uint8 device tensor of at least ``workspace_bytes(requests)``
+    bytes (256-byte aligned, as torch allocations are) that holds the interpolation
+    entries; without it the library allocates them from its own pool."""
     if not requests:
         return scratch
     dev = requests[0].ch.device
@@ -485,5 +508,9 @@ def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] 
     arr = (CRequest * n)(*[r.c_struct() for r in requests])
     st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
     with torch.cuda.device(dev):
-        _lib.call("ustb_das_fast_batch", ctypes.addressof(arr), n, scratch.data_ptr(), st)
+        if workspace is None:
+            _lib.call("ustb_das_fast_batch", ctypes.addressof(arr), n, scratch.data_ptr(), st)
+        else:
+            _lib.call("ustb_das_fast_batch_ws", ctypes.addressof(arr), n, scratch.data_ptr(), workspace.data_ptr(),
+                      workspace.numel() * workspace.element_size(), st)
     return scratch
