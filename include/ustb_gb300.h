@@ -293,6 +293,21 @@ int ustb_convert_channels(const void* src, int32_t src_type, void* dst, int32_t 
                           int64_t count, float scale, void* stream);
 
 /*
+ * RF -> IQ demodulation fused with the conversion into a storage type, for the
+ * channel data the fast path consumes (+preprocess/fast_demodulation.m:121-167):
+ * iq[t][m] = sum_k taps[k] * scale * rf[t][m*D - k] * exp(-i 2 pi fc (t0 + (m*D - k)/fs))
+ * for m < ceil(L/D), rf[t][j] = 0 for j < 0; one down-mix, FIR and decimation pass.
+ * rf: n_traces x L samples (USTB_SRC_*); iq: n_traces x ceil(L/D) complex samples
+ * of the storage type (USTB_STORE_*), interleaved.  taps: device float[ntaps]
+ * (the reference designs them with kaiserord + fir1 'noscale', :286-293).  The
+ * caller sets the output's initial time to t0 - (ntaps - 1) / 2 / fs and its
+ * sampling frequency to fs / D, as the reference does (:170-175).
+ */
+int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32_t dst_type, int64_t L,
+                    int64_t n_traces, double fs, double t0, double fc, int32_t decimation,
+                    const float* taps, int32_t ntaps, float scale, void* stream);
+
+/*
  * FIR filter along depth with delay compensation, for the band-pass step of the
  * simplified-DMAS post-process (+postprocess/simplified_delay_multiply_and_sum.m:170-176):
  * out[c][z] = sum_k taps[k] * in[c][z + delay - k], zero outside [0, nz).

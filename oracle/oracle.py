@@ -16,6 +16,10 @@ What is here:
 * ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
                      +postprocess/coherence_factor.m:100-135 and of the per-pixel
                      term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
+* ``fast_demodulation_f64`` — FP64 numpy restatement of the down-mix, causal FIR
+                     and decimation of +preprocess/fast_demodulation.m:121-167.
+                     Parity unpinned: the reference ships no golden vectors for
+                     this step and MATLAB is not available to run it.
 
 Array convention: every array is given with its MATLAB logical shape
 (channel data [L, N, W, F], tables [P, W] / [P, N]) and is passed to C in
@@ -193,3 +197,16 @@ def sdmas_filtered(y, taps):
     pad = np.concatenate([y, np.zeros((d,) + y.shape[1:])], axis=0)
     f = lfilter(taps, 1.0, pad, axis=0)[d:]
     return hilbert(f, axis=0)
+
+
+def fast_demodulation_f64(rf, fs, t0, fc, taps, decimation):
+    """IQ of real RF ``rf`` [L, ...] (time first, as MATLAB stores channel data):
+    data .* exp(-1j*2*pi*fc*time) (fast_demodulation.m:121), filter(b, 1, data, [], 1)
+    (:140), data(1:D:end, ...) (:162), all in double precision."""
+    from scipy.signal import lfilter
+
+    x = np.asarray(rf, np.float64)
+    t = float(t0) + np.arange(x.shape[0]) / float(fs)
+    mix = np.exp(-1j * 2 * np.pi * float(fc) * t).reshape((-1,) + (1,) * (x.ndim - 1))
+    y = lfilter(np.asarray(taps, np.float64), [1.0], x * mix, axis=0)
+    return y[::int(decimation)]

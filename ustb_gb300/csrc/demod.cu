@@ -1,0 +1,168 @@
+// RF -> IQ demodulation fused with the conversion into the fast path's storage type:
+// down-mix, low-pass FIR and decimation in one pass over the RF samples
+// (+preprocess/fast_demodulation.m:121-167 and :286-293 for the filter):
+//
+//   mix[j] = scale * x[j] * exp(-i 2 pi fc t_j),   t_j = t0 + j / fs
+//   y[m]   = sum_k b[k] * mix[m*D - k]              (causal FIR, zero before j = 0)
+//
+// for m = 0 .. ceil(L/D) - 1 (MATLAB's data(1:D:end,...)).  The caller shifts the
+// output's initial time by the filter delay (ntaps - 1) / 2 / fs.
+//
+// One CTA computes kOut consecutive outputs of one trace: it stages the mixed
+// samples they need (kOut*D + ntaps - 1 of them) in shared memory, one sample per
+// thread, then each thread forms outputs from shared memory.  The mixer phase
+// is formed in cycles as c0 + j*step with step split into two floats and the
+// product's rounding error recovered by an FMA, so the phase stays exact to
+// ~1e-7 cycles over any trace length.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int kOut = 256;     // outputs per CTA
+constexpr int kThreads = 256;
+
+template <typename S>
+__device__ __forceinline__ float rf_sample(const S* p, int64_t i);
+template <>
+__device__ __forceinline__ float rf_sample<float>(const float* p, int64_t i) { return __ldg(p + i); }
+template <>
+__device__ __forceinline__ float rf_sample<int16_t>(const int16_t* p, int64_t i) { return (float)__ldg(p + i); }
+template <>
+__device__ __forceinline__ float rf_sample<__half>(const __half* p, int64_t i) { return __half2float(__ldg(p + i)); }
+
+template <typename D>
+__device__ __forceinline__ void store_iq(D* out, int64_t i, float2 v);
+template <>
+__device__ __forceinline__ void store_iq<float>(float* out, int64_t i, float2 v) {
+    reinterpret_cast<float2*>(out)[i] = v;
+}
+template <>
+__device__ __forceinline__ void store_iq<__half>(__half* out, int64_t i, float2 v) {
+    reinterpret_cast<__half2*>(out)[i] = __floats2half2_rn(v.x, v.y);
+}
+template <>
+__device__ __forceinline__ void store_iq<__nv_bfloat16>(__nv_bfloat16* out, int64_t i, float2 v) {
+    reinterpret_cast<__nv_bfloat162*>(out)[i] = __floats2bfloat162_rn(v.x, v.y);
+}
+
+struct DemodArgs {
+    int64_t L, Ld, n_traces;
+    int D, ntaps;
+    float c0;              // fractional part of fc * t0 (cycles)
+    float step_hi, step_lo;  // fc / fs split into two floats
+    float scale;
+};
+
+template <typename S, typename D>
+__global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ rf, D* __restrict__ iq,
+                                                         const float* __restrict__ taps, const DemodArgs a) {
+    extern __shared__ float2 mix[];  // [kOut * D + ntaps - 1]
+    const int64_t chunks = (a.Ld + kOut - 1) / kOut;
+    const int64_t trace = blockIdx.x / chunks;
+    const int64_t m0 = (blockIdx.x - trace * chunks) * kOut;
+    if (trace >= a.n_traces) return;
+    const S* x = rf + trace * a.L;
+    const int64_t j0 = m0 * a.D - (a.ntaps - 1);  // first staged sample (may be negative)
+    const int nstage = kOut * a.D + a.ntaps - 1;
+    for (int s = threadIdx.x; s < nstage; s += kThreads) {
+        const int64_t j = j0 + s;
+        float2 v = make_float2(0.f, 0.f);
+        if (j >= 0 && j < a.L) {
+            const float jf = (float)j;  // exact: L < 2^24
+            const float p = jf * a.step_hi;
+            const float e = fmaf(jf, a.step_hi, -p);  // rounding error of the product
+            const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
+            float sn, cs;
+            __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
+            const float r = a.scale * rf_sample<S>(x, j);
+            v = make_float2(r * cs, r * sn);
+        }
+        mix[s] = v;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < kOut; o += kThreads) {
+        const int64_t m = m0 + o;
+        if (m >= a.Ld) break;
+        // y[m] = sum_k b[k] mix[m*D - k]; in the staged window m*D - k sits at o*D + ntaps-1 - k
+        const float2* w = mix + (int64_t)o * a.D + a.ntaps - 1;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = 0; k < a.ntaps; ++k) {
+            const float b = __ldg(taps + k);
+            const float2 v = w[-k];
+            acc.x = fmaf(b, v.x, acc.x);
+            acc.y = fmaf(b, v.y, acc.y);
+        }
+        store_iq<D>(iq, trace * a.Ld + m, acc);
+    }
+}
+
+template <typename S>
+int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, const DemodArgs& a, cudaStream_t s) {
+    const int64_t chunks = (a.Ld + kOut - 1) / kOut;
+    const int64_t blocks = chunks * a.n_traces;
+    USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
+    const size_t smem = sizeof(float2) * (size_t)(kOut * a.D + a.ntaps - 1);
+    int dev = 0, optin = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "decimation %d with %d taps needs %zu bytes of shared memory",
+                 a.D, a.ntaps, smem);
+    switch (dst_type) {
+        case USTB_STORE_F32:
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, float><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (float*)iq, taps, a);
+            break;
+        case USTB_STORE_F16:
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, __half><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__half*)iq, taps, a);
+            break;
+        default:
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, __nv_bfloat16><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__nv_bfloat16*)iq, taps, a);
+            break;
+    }
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
+}  // namespace
+
+extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32_t dst_type, int64_t L,
+                               int64_t n_traces, double fs, double t0, double fc, int32_t decimation,
+                               const float* taps, int32_t ntaps, float scale, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(src_type >= 0 && src_type <= 2, USTB_E_DTYPE, "unknown source type %d", (int)src_type);
+    USTB_REQUIRE(dst_type >= 0 && dst_type <= 2, USTB_E_DTYPE, "unknown storage type %d", (int)dst_type);
+    USTB_REQUIRE(L >= 0 && n_traces >= 0, USTB_E_SHAPE, "negative size");
+    USTB_REQUIRE(L < (1 << 24), USTB_E_SHAPE, "at most 2^24 samples per trace");
+    USTB_REQUIRE(decimation >= 1 && decimation <= 64, USTB_E_ARG, "decimation must be in [1, 64], got %d",
+                 (int)decimation);
+    USTB_REQUIRE(ntaps >= 1 && ntaps <= 4096, USTB_E_ARG, "ntaps must be in [1, 4096], got %d", (int)ntaps);
+    USTB_REQUIRE(fs > 0.0, USTB_E_ARG, "sampling frequency must be > 0");
+    if (L == 0 || n_traces == 0) return USTB_OK;
+    USTB_REQUIRE(rf && iq && taps, USTB_E_ARG, "NULL pointer");
+    DemodArgs a;
+    a.L = L;
+    a.Ld = (L + decimation - 1) / decimation;
+    a.n_traces = n_traces;
+    a.D = decimation;
+    a.ntaps = ntaps;
+    const double c0 = fc * t0;
+    a.c0 = (float)(c0 - std::floor(c0));
+    const double step = fc / fs;
+    a.step_hi = (float)step;
+    a.step_lo = (float)(step - (double)a.step_hi);
+    a.scale = scale;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (src_type) {
+        case USTB_SRC_F32: return launch_demod<float>((const float*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_I16: return launch_demod<int16_t>((const int16_t*)rf, iq, dst_type, taps, a, s);
+        default: return launch_demod<__half>((const __half*)rf, iq, dst_type, taps, a, s);
+    }
+}
