@@ -308,6 +308,21 @@ int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32_t dst_type
                     const float* taps, int32_t ntaps, float scale, void* stream);
 
 /*
+ * Headless image formation of a sector-scan result: envelope and compression
+ * (+uff/beamformed_data.m:300-316 get_image: 0 = log, 20 log10(|b| / max|b|) with the
+ * maximum over all frames; 1 = sqrt(|b|); 2 = |b|), then scan conversion onto a
+ * uniform Cartesian grid by bilinear interpolation in (azimuth, depth) with -inf
+ * outside the sector (+tools/scan_convert.m).  data: [n_depth, n_azimuth, n_frames]
+ * (depth fastest) complex or real single; depth/azimuth axes: increasing device
+ * float arrays; out: [n_frames][size_x][size_z] floats (z fastest), pixel (ix, iz) at
+ * x = x0 + ix*dx, z = z0 + iz*dz.  peak: device float that receives max|b| (log only).
+ */
+int ustb_scan_convert(const void* data, int32_t is_complex, int32_t compression, int64_t n_depth,
+                      int64_t n_azimuth, int64_t n_frames, const float* depth_axis,
+                      const float* azimuth_axis, float* peak, float* out, int64_t size_x,
+                      int64_t size_z, float x0, float dx, float z0, float dz, void* stream);
+
+/*
  * FIR filter along depth with delay compensation, for the band-pass step of the
  * simplified-DMAS post-process (+postprocess/simplified_delay_multiply_and_sum.m:170-176):
  * out[c][z] = sum_k taps[k] * in[c][z + delay - k], zero outside [0, nz).

@@ -16,6 +16,10 @@ What is here:
 * ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
                      +postprocess/coherence_factor.m:100-135 and of the per-pixel
                      term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
+* ``scan_convert_f64`` — FP64 numpy restatement of get_image's compression
+                     (+uff/beamformed_data.m:300-316) and +tools/scan_convert.m
+                     (bilinear interp2 in (azimuth, depth), -inf outside).  Parity
+                     unpinned: no golden vectors in the reference.
 * ``fast_demodulation_f64`` — FP64 numpy restatement of the down-mix, causal FIR
                      and decimation of +preprocess/fast_demodulation.m:121-167.
                      Parity unpinned: the reference ships no golden vectors for
@@ -210,3 +214,34 @@ def fast_demodulation_f64(rf, fs, t0, fc, taps, decimation):
     mix = np.exp(-1j * 2 * np.pi * float(fc) * t).reshape((-1,) + (1,) * (x.ndim - 1))
     y = lfilter(np.asarray(taps, np.float64), [1.0], x * mix, axis=0)
     return y[::int(decimation)]
+
+
+def scan_convert_f64(img, depth_axis, azimuth_axis, xs, zs, compression="log"):
+    """Compressed image [n_depth, n_azimuth, F] (|.| of complex or real data) on the
+    Cartesian grid (xs, zs): returns [F, len(zs), len(xs)], -inf outside the sector.
+    Follows scan_convert.m: cart2pol(Zs, Xs) -> theta = atan2(x, z), r = hypot(x, z);
+    interp2(thetaGrid, rangeGrid, image, theta, r, 'linear', -inf)."""
+    a = np.abs(np.asarray(img)).astype(np.float64)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    if compression == "log":
+        v = 20 * np.log10(a / a.max())
+    elif compression == "sqrt":
+        v = np.sqrt(a)
+    else:
+        v = a
+    d = np.asarray(depth_axis, np.float64)
+    t = np.asarray(azimuth_axis, np.float64)
+    X, Z = np.meshgrid(np.asarray(xs, np.float64), np.asarray(zs, np.float64))
+    th, r = np.arctan2(X, Z), np.hypot(X, Z)
+    out = np.full((v.shape[2],) + X.shape, -np.inf)
+    ok = (r >= d[0]) & (r <= d[-1]) & (th >= t[0]) & (th <= t[-1])
+    i = np.clip(np.searchsorted(d, r[ok], side="right") - 1, 0, d.size - 2)
+    j = np.clip(np.searchsorted(t, th[ok], side="right") - 1, 0, t.size - 2)
+    u = (r[ok] - d[i]) / (d[i + 1] - d[i])
+    w = (th[ok] - t[j]) / (t[j + 1] - t[j])
+    for f in range(v.shape[2]):
+        vf = v[:, :, f]
+        out[f][ok] = ((1 - u) * ((1 - w) * vf[i, j] + w * vf[i, j + 1])
+                      + u * ((1 - w) * vf[i + 1, j] + w * vf[i + 1, j + 1]))
+    return out
