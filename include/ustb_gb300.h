@@ -323,6 +323,28 @@ int ustb_scan_convert(const void* data, int32_t is_complex, int32_t compression,
                       int64_t size_z, float x0, float dx, float z0, float dz, void* stream);
 
 /*
+ * Phase coherence factor on a kept cube (+postprocess/phase_coherence_factor.m:64-129):
+ * cube [F][K][P] complex single (pixel fastest: the channels of a dimension.transmit
+ * result, or the waves of a dimension.receive one), weights [K][P] (the apodization
+ * of the summed dimension, as MATLAB's [P, K]) or NULL for ones.  Outputs [F][P]
+ * (any may be NULL): fca = max(0, 1 - gamma/sigma0 * min(std phase, std shifted
+ * phase)), fcc = 1 - sqrt(var cos + var sin) (weighted, tools/weigthed_std.m),
+ * image = fcc * sum.  The optional centre-frequency re-phasing of the reference is
+ * not applied.
+ */
+int ustb_phase_coherence(const void* cube, int64_t P, int64_t K, int64_t F, const float* weights,
+                         float gamma, float sigma0, float* fca, float* fcc, void* image, void* stream);
+
+/*
+ * Generalized coherence factor on a kept cube
+ * (+postprocess/generalized_coherence_factor.m:66-97): gcf = energy of the DFT bins
+ * [0..M0] and [K-M0..K-1] (only bin 0 when M0 <= 1) over the total energy along the
+ * K values of each pixel; image = gcf * sum.  Layout as ustb_phase_coherence.
+ */
+int ustb_generalized_coherence(const void* cube, int64_t P, int64_t K, int64_t F, int32_t M0, float* gcf,
+                               void* image, void* stream);
+
+/*
  * FIR filter along depth with delay compensation, for the band-pass step of the
  * simplified-DMAS post-process (+postprocess/simplified_delay_multiply_and_sum.m:170-176):
  * out[c][z] = sum_k taps[k] * in[c][z + delay - k], zero outside [0, nz).

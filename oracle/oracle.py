@@ -16,6 +16,11 @@ What is here:
 * ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
                      +postprocess/coherence_factor.m:100-135 and of the per-pixel
                      term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
+* ``phase_coherence_factor_f64`` / ``generalized_coherence_factor_f64`` — FP64
+                     numpy restatements of +postprocess/phase_coherence_factor.m:64-129
+                     (with tools/weigthed_std.m, weigthed_var.m, weigthed_mean.m) and
+                     +postprocess/generalized_coherence_factor.m:66-97 over one
+                     dimension.  Parity unpinned (no golden vectors in the reference).
 * ``scan_convert_f64`` — FP64 numpy restatement of get_image's compression
                      (+uff/beamformed_data.m:300-316) and +tools/scan_convert.m
                      (bilinear interp2 in (azimuth, depth), -inf outside).  Parity
@@ -245,3 +250,37 @@ def scan_convert_f64(img, depth_axis, azimuth_axis, xs, zs, compression="log"):
         out[f][ok] = ((1 - u) * ((1 - w) * vf[i, j] + w * vf[i, j + 1])
                       + u * ((1 - w) * vf[i + 1, j] + w * vf[i + 1, j + 1]))
     return out
+
+
+def _wmean(D, W, axis):
+    return (W * D).sum(axis) / W.sum(axis)
+
+
+def _wvar(D, W, axis):
+    m = np.expand_dims(_wmean(D, W, axis), axis)
+    return (W * (D - m) ** 2).sum(axis) / W.sum(axis)
+
+
+def phase_coherence_factor_f64(data, weights=None, gamma=1.0, sigma_0=np.pi / np.sqrt(3), axis=1):
+    """FCA, FCC and FCC * coherent sum over ``axis`` of complex ``data`` (e.g. [P, K])."""
+    d = np.asarray(data, np.complex128)
+    W = np.ones(d.shape) if weights is None else np.broadcast_to(np.asarray(weights, np.float64), d.shape)
+    phase = np.angle(d)
+    aux = np.where(phase <= 0, phase + np.pi, phase - np.pi)
+    sf = np.minimum(np.sqrt(_wvar(phase, W, axis)), np.sqrt(_wvar(aux, W, axis)))
+    fca = 1 - (gamma / sigma_0) * sf
+    fca[fca < 0] = 0
+    fca[np.isnan(fca)] = 0
+    fcc = 1 - np.sqrt(_wvar(np.cos(phase), W, axis) + _wvar(np.sin(phase), W, axis))
+    return fca, fcc, fcc * d.sum(axis)
+
+
+def generalized_coherence_factor_f64(data, M0=4, axis=1):
+    """GCF and GCF * coherent sum over ``axis`` of complex ``data``."""
+    d = np.asarray(data, np.complex128)
+    K = d.shape[axis]
+    idx = np.r_[0:M0 + 1, K - M0:K] if M0 > 1 else np.array([0])
+    X = np.abs(np.fft.fft(d, axis=axis)) ** 2
+    g = np.take(X, idx, axis=axis).sum(axis) / X.sum(axis)
+    g[np.isnan(g)] = 0
+    return g, g * d.sum(axis)

@@ -1,4 +1,5 @@
-"""Post-DAS steps that follow the fused coherence-factor / simplified-DMAS epilogue.
+"""Post-DAS steps: the follow-up of the fused coherence-factor / simplified-DMAS
+epilogue, and the phase / generalized coherence factors on a kept cube.
 
 ``simplified_dmas_image`` completes +postprocess/simplified_delay_multiply_and_sum.m
 on a linear scan: the per-pixel value ((sum sign(s) sqrt|s|)^2 - sum |s|)/2
@@ -121,3 +122,47 @@ def simplified_dmas_image(sdmas: torch.Tensor, nz: int, nx: int, z_step: float, 
     y = sdmas.reshape(-1, nx, nz).to(torch.float32)
     filt = fir_depth(y.reshape(-1, nz), taps).reshape(-1, nx, nz)
     return hilbert_depth(filt).reshape(sdmas.shape[0], -1)
+
+
+def _cube_fkp(cube: torch.Tensor) -> torch.Tensor:
+    """ABI cube (F, W|1, N|1, P) with one of W, N equal to 1 -> contiguous (F, K, P)."""
+    if cube.dim() != 4 or not cube.is_complex():
+        raise TypeError("cube must be a complex (F, W, N, P) tensor")
+    F, W, N, P = cube.shape
+    if W > 1 and N > 1:
+        raise ValueError("the factor runs over one dimension: give a dimension.transmit or .receive cube")
+    return cube.reshape(F, W * N, P).to(torch.complex64).contiguous()
+
+
+def phase_coherence_factor(cube: torch.Tensor, weights: Optional[torch.Tensor] = None, gamma: float = 1.0,
+                           sigma_0: float = math.pi / math.sqrt(3)):
+    """Phase coherence factor (+postprocess/phase_coherence_factor.m) over the kept
+    dimension of ``cube`` (ABI layout (F, W|1, N|1, P) complex).  ``weights``: (K, P)
+    apodization of that dimension or None.  Returns dict of (F, P) tensors 'FCA',
+    'FCC' and 'image' (= FCC * coherent sum)."""
+    c = _cube_fkp(cube)
+    F, K, P = c.shape
+    dev = c.device
+    w = None if weights is None else weights.to(torch.float32).reshape(K, P).contiguous()
+    out = {"FCA": torch.empty((F, P), dtype=torch.float32, device=dev),
+           "FCC": torch.empty((F, P), dtype=torch.float32, device=dev),
+           "image": torch.empty((F, P), dtype=torch.complex64, device=dev)}
+    with torch.cuda.device(dev):
+        _lib.call("ustb_phase_coherence", c.data_ptr(), P, K, F, 0 if w is None else w.data_ptr(), float(gamma),
+                  float(sigma_0), out["FCA"].data_ptr(), out["FCC"].data_ptr(), out["image"].data_ptr(),
+                  torch.cuda.current_stream(dev).cuda_stream)
+    return out
+
+
+def generalized_coherence_factor(cube: torch.Tensor, M0: int = 4):
+    """Generalized coherence factor (+postprocess/generalized_coherence_factor.m) over
+    the kept dimension of ``cube``.  Returns dict of (F, P) tensors 'GCF' and 'image'."""
+    c = _cube_fkp(cube)
+    F, K, P = c.shape
+    dev = c.device
+    out = {"GCF": torch.empty((F, P), dtype=torch.float32, device=dev),
+           "image": torch.empty((F, P), dtype=torch.complex64, device=dev)}
+    with torch.cuda.device(dev):
+        _lib.call("ustb_generalized_coherence", c.data_ptr(), P, K, F, int(M0), out["GCF"].data_ptr(),
+                  out["image"].data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+    return out
