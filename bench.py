@@ -441,7 +441,8 @@ def main():
     ap.add_argument("--no-hfr", action="store_true", help="skip the high-frame-rate ensemble section")
     ap.add_argument("--serving-requests", type=int, default=200)
     ap.add_argument("--profile", default=None, metavar="WORKLOAD",
-                    help="launch only the kernels of one workload (headline or a synth.CONFIGS name) "
+                    help="launch only the kernels of one workload (headline, a synth.CONFIGS name, or "
+                         "demod / image / coherence for the kernels around the beamformer) "
                          "--steps times each, for ncu; prints their CUDA-event times")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "bf16"],
                     help="channel storage of the fast kernel under --profile")
@@ -598,10 +599,61 @@ def main():
     print(json.dumps(res), flush=True)
 
 
+def profile_post(args, torch):
+    """--profile demod | image | coherence: the kernels around the beamformer.
+
+    demod:     20 frames x 11 waves x 128 channels x 3072 int16 RF samples (fs 40 MHz,
+               f0 5 MHz) -> IQ at fs/4 in FP16 (ustb_demodulate);
+    image:     the diverging-wave sector image (256 azimuths x 512 depths) -> 512 x 512
+               log-compressed Cartesian image (ustb_scan_convert);
+    coherence: its 64-channel cube (dimension.transmit) -> phase and generalized
+               coherence factors."""
+    from ustb_gb300 import fast, image, postprocess, preprocess, synth
+    from ustb_gb300.das import channel_tensor
+    from ustb_gb300.enums import Precision
+
+    dev = torch.device("cuda", 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"profile": args.profile}
+    if args.profile == "demod":
+        g = torch.Generator(device=dev).manual_seed(7)
+        rf = (torch.randn((20, 11, 128, 3072), generator=g, device=dev) * 3000).to(torch.int16)
+        fs, fc = 40e6, 5e6
+        taps = preprocess.lowpass_taps(fc, fs)
+        D, _ = preprocess.decimation_factor(fs, 2 * fc)
+        fn = lambda: preprocess.demodulate(rf, fs, 0.0, fc, taps, D, Precision.fp16, 1 / 3000)
+        out.update(samples=int(rf.numel()), ntaps=int(len(taps)), decimation=D,
+                   bytes=int(rf.numel() * 2 + (rf.numel() // D) * 4))
+    else:
+        wl = synth.config_dw_sector(device=dev)
+        das = build_das(wl)
+        geom = das.fast_geometry(dev)
+        ch = channel_tensor(wl.channel_data.data, dev)
+        st = fast.convert_channels(ch, Precision.fp16)
+        o = fast.das_fast(st, Precision.fp16, True, geom, int(wl.dimension), L=ch.shape[-1], epilogue=True)
+        torch.cuda.synchronize()
+        if args.profile == "image":
+            img = o["das"][0]
+            fn = lambda: image.scan_convert(img, wl.scan)
+            out.update(pixels_in=int(img.numel()), pixels_out=512 * 512)
+        else:
+            cube = o["cube"]
+            fn = lambda: (postprocess.phase_coherence_factor(cube), postprocess.generalized_coherence_factor(cube))
+            out.update(cube_bytes=int(cube.numel() * 8))
+    for _ in range(args.warmup):
+        fn()
+    out["ms"] = [round(t, 4) for t in cuda_time(fn, args.steps, flush, stream, torch)]
+    print(json.dumps(out), flush=True)
+
+
 def main_profile(args):
     """A short run for ncu: the fast kernel, then the das_c-exact table kernel, on one
     workload, ``--steps`` launches each after ``--warmup`` warm-up launches each."""
     import torch
+
+    if args.profile in ("demod", "image", "coherence"):
+        return profile_post(args, torch)
 
     from ustb_gb300 import fast, geometry, kernels, synth
     from ustb_gb300.enums import Precision

@@ -8,14 +8,17 @@
 //   std(x) = sqrt(sum w (x - mean_w x)^2 / sum w)     (tools/weigthed_std.m)
 //   FCA = max(0, 1 - gamma / sigma0 * min(std phi, std psi))   (NaN -> 0)
 //   FCC = 1 - sqrt(var_w(cos phi) + var_w(sin phi)),  image = FCC * sum s
-// computed in two passes over the K values, as the reference's mean-then-variance.
+// computed in one pass with weighted incremental updates (the reference's
+// mean-then-variance to rounding), four threads per pixel over a quarter of the K
+// values each, merged pairwise.
 //
 // Generalized coherence factor (+postprocess/generalized_coherence_factor.m:66-97):
 //   GCF = sum_{k in LF} |DFT_K(s)[k]|^2 / sum_k |DFT_K(s)[k]|^2   (NaN -> 0),
 //   LF = MATLAB indices [1:M0+1, K-M0+1:K] (repeats counted twice, as indexing does)
 //   when M0 > 1, else [1];  image = GCF * sum s.  The total is K * sum |s|^2
-//   (Parseval); the low-frequency bins are DFTs over a twiddle table in shared memory.
-//   K <= 4096 keeps that table within the default 48 KB.
+//   (Parseval); the low-frequency bins (at most 15: M0 <= 7) are DFTs over a twiddle
+//   table in shared memory, summed in registers by four threads per pixel.  K <= 1024
+//   keeps that table and the partial sums within the default 48 KB.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,53 +31,91 @@ namespace {
 constexpr int kThreads = 256;
 constexpr float kPi = 3.14159265358979f;
 
+constexpr int kParts = 4;                    // threads per pixel, each over a quarter of K
+constexpr int kPix = kThreads / kParts;      // pixels per CTA (64: two warps of pixels per part)
+
+// weighted running mean and sum of squared deviations (West's incremental update,
+// the algorithm of tools/weighted_incremental_variance.m): var = S / W; partial runs
+// merge exactly (Chan et al.'s pairwise update)
+struct WRun {
+    float mean = 0.f, S = 0.f;
+    __device__ __forceinline__ void add(float x, float w, float w_over_W) {
+        const float d = x - mean;
+        mean = fmaf(w_over_W, d, mean);
+        S = fmaf(w * d, x - mean, S);
+    }
+    __device__ __forceinline__ void merge(float Wa, float Wb, float mb, float Sb) {
+        const float Wt = Wa + Wb;
+        if (Wb == 0.f) return;
+        if (Wa == 0.f) { mean = mb; S = Sb; return; }
+        const float d = mb - mean;
+        mean = fmaf(d, Wb / Wt, mean);
+        S = S + Sb + d * d * (Wa * Wb / Wt);
+    }
+};
+
+// CTA layout: thread = (part g, pixel slot i), g = tid / kPix, i = tid % kPix, so a
+// warp reads 32 consecutive pixels of one k (coalesced); part g takes k = g, g+4, ...
 __global__ void __launch_bounds__(kThreads) pcf_kernel(const float2* __restrict__ cube, const float* __restrict__ wts,
                                                        int64_t P, int64_t K, int64_t F, float gamma_over_sigma,
                                                        float* fca, float* fcc, float2* image) {
+    __shared__ float red[kParts][11][kPix];
+    const int g = threadIdx.x / kPix, i = threadIdx.x % kPix;
     const int64_t total = P * F;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t f = t / P, p = t - f * P;
+    for (int64_t t0 = (int64_t)blockIdx.x * kPix; t0 < total; t0 += (int64_t)gridDim.x * kPix) {
+        const int64_t t = t0 + i;
+        const bool ok = t < total;
+        const int64_t f = ok ? t / P : 0, p = ok ? t - f * P : 0;
         const float2* s = cube + f * K * P + p;
-        float sw = 0.f, sphi = 0.f, spsi = 0.f, sc = 0.f, ss = 0.f;
+        float W = 0.f;
+        WRun rphi, rpsi, rc, rs;
         float2 sum = make_float2(0.f, 0.f);
-        for (int64_t k = 0; k < K; ++k) {
-            const float2 v = __ldg(s + k * P);
-            const float w = wts ? __ldg(wts + k * P + p) : 1.f;
-            const float phi = atan2f(v.y, v.x);
-            const float psi = phi <= 0.f ? phi + kPi : phi - kPi;
-            float sn, cs;
-            sincosf(phi, &sn, &cs);
-            sw += w;
-            sphi += w * phi;
-            spsi += w * psi;
-            sc += w * cs;
-            ss += w * sn;
-            sum.x += v.x;
-            sum.y += v.y;
+        if (ok) {
+            for (int64_t k = g; k < K; k += kParts) {
+                const float2 v = __ldg(s + k * P);
+                const float w = wts ? __ldg(wts + k * P + p) : 1.f;
+                sum.x += v.x;
+                sum.y += v.y;
+                if (w == 0.f) continue;  // zero weight: no change to any weighted statistic
+                W += w;
+                const float q = w / W;
+                const float phi = atan2f(v.y, v.x);
+                const float psi = phi <= 0.f ? phi + kPi : phi - kPi;
+                float sn, cs;
+                sincosf(phi, &sn, &cs);
+                rphi.add(phi, w, q);
+                rpsi.add(psi, w, q);
+                rc.add(cs, w, q);
+                rs.add(sn, w, q);
+            }
         }
-        const float inv = 1.f / sw;
-        const float mphi = sphi * inv, mpsi = spsi * inv, mc = sc * inv, ms = ss * inv;
-        float vphi = 0.f, vpsi = 0.f, vcs = 0.f;
-        for (int64_t k = 0; k < K; ++k) {
-            const float2 v = __ldg(s + k * P);
-            const float w = wts ? __ldg(wts + k * P + p) : 1.f;
-            const float phi = atan2f(v.y, v.x);
-            const float psi = phi <= 0.f ? phi + kPi : phi - kPi;
-            float sn, cs;
-            sincosf(phi, &sn, &cs);
-            vphi += w * (phi - mphi) * (phi - mphi);
-            vpsi += w * (psi - mpsi) * (psi - mpsi);
-            vcs += w * ((cs - mc) * (cs - mc) + (sn - ms) * (sn - ms));
+        const float v11[11] = {W, rphi.mean, rphi.S, rpsi.mean, rpsi.S, rc.mean, rc.S, rs.mean, rs.S, sum.x, sum.y};
+#pragma unroll
+        for (int j = 0; j < 11; ++j) red[g][j][i] = v11[j];
+        __syncthreads();
+        if (g == 0 && ok) {
+            for (int h = 1; h < kParts; ++h) {
+                const float Wb = red[h][0][i];
+                rphi.merge(W, Wb, red[h][1][i], red[h][2][i]);
+                rpsi.merge(W, Wb, red[h][3][i], red[h][4][i]);
+                rc.merge(W, Wb, red[h][5][i], red[h][6][i]);
+                rs.merge(W, Wb, red[h][7][i], red[h][8][i]);
+                W += Wb;
+                sum.x += red[h][9][i];
+                sum.y += red[h][10][i];
+            }
+            const float inv = 1.f / W;  // W = 0: NaN statistics, as the reference's 0/0
+            const float sf = fminf(sqrtf(rphi.S * inv), sqrtf(rpsi.S * inv));
+            float a = 1.f - gamma_over_sigma * sf;
+            if (a < 0.f) a = 0.f;
+            if (a != a) a = 0.f;
+            const float c = 1.f - sqrtf((rc.S + rs.S) * inv);
+            const int64_t o = f * P + p;
+            if (fca) fca[o] = a;
+            if (fcc) fcc[o] = c;
+            if (image) image[o] = make_float2(c * sum.x, c * sum.y);
         }
-        const float sf = fminf(sqrtf(vphi * inv), sqrtf(vpsi * inv));
-        float a = 1.f - gamma_over_sigma * sf;
-        if (a < 0.f) a = 0.f;
-        if (a != a) a = 0.f;
-        const float c = 1.f - sqrtf(vcs * inv);
-        const int64_t o = f * P + p;
-        if (fca) fca[o] = a;
-        if (fcc) fcc[o] = c;
-        if (image) image[o] = make_float2(c * sum.x, c * sum.y);
+        __syncthreads();
     }
 }
 
@@ -83,55 +124,88 @@ struct Bins {
     int b[64];
 };
 
+template <int NB>  // number of low-frequency bins, 1 or 2 M0 + 1
 __global__ void __launch_bounds__(kThreads) gcf_kernel(const float2* __restrict__ cube, int64_t P, int64_t K,
                                                        int64_t F, const Bins bins, float* gcf, float2* image) {
     extern __shared__ float2 tw[];  // tw[m] = exp(-i 2 pi m / K)
+    __shared__ float2 red[kParts][NB + 1][kPix];
+    __shared__ float rede[kParts][kPix];
     for (int m = threadIdx.x; m < K; m += blockDim.x) {
         float sn, cs;
         sincospif(-2.f * (float)m / (float)K, &sn, &cs);
         tw[m] = make_float2(cs, sn);
     }
     __syncthreads();
+    const int g = threadIdx.x / kPix, i = threadIdx.x % kPix;
     const int64_t total = P * F;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t f = t / P, p = t - f * P;
+    for (int64_t t0 = (int64_t)blockIdx.x * kPix; t0 < total; t0 += (int64_t)gridDim.x * kPix) {
+        const int64_t t = t0 + i;
+        const bool ok = t < total;
+        const int64_t f = ok ? t / P : 0, p = ok ? t - f * P : 0;
         const float2* s = cube + f * K * P + p;
         float e = 0.f;
         float2 sum = make_float2(0.f, 0.f);
-        for (int64_t k = 0; k < K; ++k) {
-            const float2 v = __ldg(s + k * P);
-            e += v.x * v.x + v.y * v.y;
-            sum.x += v.x;
-            sum.y += v.y;
-        }
-        float lf = 0.f;
-        for (int b = 0; b < bins.n; ++b) {
+        float2 X[NB];
+        int mb[NB], step[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            X[b] = make_float2(0.f, 0.f);
             const int bin = bins.b[b];
-            float2 X = make_float2(0.f, 0.f);
-            int m = 0;  // bin * k mod K
-            for (int64_t k = 0; k < K; ++k) {
-                const float2 v = __ldg(s + k * P);
-                const float2 w = tw[m];
-                X.x += v.x * w.x - v.y * w.y;
-                X.y += v.x * w.y + v.y * w.x;
-                m += bin;
-                if (m >= K) m -= (int)K;
-            }
-            lf += X.x * X.x + X.y * X.y;
+            mb[b] = (int)(((int64_t)bin * g) % K);             // twiddle index of k = g
+            step[b] = (int)(((int64_t)bin * kParts) % K);      // advance per k += kParts
         }
-        float g = lf / ((float)K * e);
-        if (g != g) g = 0.f;
-        const int64_t o = f * P + p;
-        if (gcf) gcf[o] = g;
-        if (image) image[o] = make_float2(g * sum.x, g * sum.y);
+        if (ok) {
+            for (int64_t k = g; k < K; k += kParts) {
+                const float2 v = __ldg(s + k * P);
+                e += v.x * v.x + v.y * v.y;
+                sum.x += v.x;
+                sum.y += v.y;
+#pragma unroll
+                for (int b = 0; b < NB; ++b) {
+                    const float2 w = tw[mb[b]];
+                    X[b].x += v.x * w.x - v.y * w.y;
+                    X[b].y += v.x * w.y + v.y * w.x;
+                    mb[b] += step[b];
+                    if (mb[b] >= K) mb[b] -= (int)K;
+                }
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b) red[g][b][i] = X[b];
+        red[g][NB][i] = sum;
+        rede[g][i] = e;
+        __syncthreads();
+        if (g == 0 && ok) {
+            float lf = 0.f;
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                float2 x = X[b];
+                for (int h = 1; h < kParts; ++h) {
+                    x.x += red[h][b][i].x;
+                    x.y += red[h][b][i].y;
+                }
+                lf += x.x * x.x + x.y * x.y;
+            }
+            for (int h = 1; h < kParts; ++h) {
+                e += rede[h][i];
+                sum.x += red[h][NB][i].x;
+                sum.y += red[h][NB][i].y;
+            }
+            float gv = lf / ((float)K * e);
+            if (gv != gv) gv = 0.f;
+            const int64_t o = f * P + p;
+            if (gcf) gcf[o] = gv;
+            if (image) image[o] = make_float2(gv * sum.x, gv * sum.y);
+        }
+        __syncthreads();
     }
 }
 
-unsigned grid_for(int64_t total) {
+unsigned grid_for(int64_t total) {  // CTAs of kPix pixels
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + kThreads - 1) / kThreads, (int64_t)std::max(sms, 1) * 16));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + kPix - 1) / kPix, (int64_t)std::max(sms, 1) * 32));
 }
 
 }  // namespace
@@ -156,8 +230,8 @@ extern "C" int ustb_generalized_coherence(const void* cube, int64_t P, int64_t K
     ustb::clear_error();
     USTB_REQUIRE(P >= 0 && K >= 0 && F >= 0, USTB_E_SHAPE, "negative size");
     USTB_REQUIRE(K >= 2, USTB_E_SHAPE, "Not enough channels to compute factor (K = %lld)", (long long)K);
-    USTB_REQUIRE(K <= 4096, USTB_E_SHAPE, "at most 4096 values per pixel");
-    USTB_REQUIRE(M0 >= 0 && M0 <= 31, USTB_E_ARG, "M0 must be in [0, 31]");
+    USTB_REQUIRE(K <= 1024, USTB_E_SHAPE, "at most 1024 values per pixel");
+    USTB_REQUIRE(M0 >= 0 && M0 <= 7, USTB_E_ARG, "M0 must be in [0, 7]");
     USTB_REQUIRE(M0 <= 1 || K > M0, USTB_E_SHAPE, "M0 = %d needs more than %d values per pixel (K = %lld)", (int)M0,
                  (int)M0, (long long)K);
     if (P == 0 || F == 0) return USTB_OK;
@@ -172,8 +246,19 @@ extern "C" int ustb_generalized_coherence(const void* cube, int64_t P, int64_t K
         bins.b[bins.n++] = 0;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    gcf_kernel<<<grid_for(P * F), kThreads, sizeof(float2) * (size_t)K, s>>>(static_cast<const float2*>(cube), P, K, F,
-                                                                            bins, gcf, static_cast<float2*>(image));
+    const unsigned grid = grid_for(P * F);
+    const size_t smem = sizeof(float2) * (size_t)K;
+    const float2* c = static_cast<const float2*>(cube);
+    float2* im = static_cast<float2*>(image);
+    switch (bins.n) {
+        case 1: gcf_kernel<1><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        case 5: gcf_kernel<5><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        case 7: gcf_kernel<7><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        case 9: gcf_kernel<9><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        case 11: gcf_kernel<11><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        case 13: gcf_kernel<13><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+        default: gcf_kernel<15><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
+    }
     USTB_CUDA(cudaGetLastError());
     return USTB_OK;
 }

@@ -8,9 +8,11 @@
 // for m = 0 .. ceil(L/D) - 1 (MATLAB's data(1:D:end,...)).  The caller shifts the
 // output's initial time by the filter delay (ntaps - 1) / 2 / fs.
 //
-// One CTA computes kOut consecutive outputs of one trace: it stages the mixed
-// samples they need (kOut*D + ntaps - 1 of them) in shared memory, one sample per
-// thread, then each thread forms outputs from shared memory.  The mixer phase
+// One CTA computes kout (<= 1024) consecutive outputs of one trace: it stages the
+// taps and the mixed samples the outputs need (kout*D + ntaps - 1 of them, at most
+// about 8192) in shared memory, the samples in polyphase order (phase-major) so that the
+// 32 outputs of a warp read 32 consecutive samples for each tap; each thread forms 4
+// outputs with independent accumulators.  The mixer phase
 // is formed in cycles as c0 + j*step with step split into two floats and the
 // product's rounding error recovered by an FMA, so the phase stays exact to
 // ~1e-7 cycles over any trace length.
@@ -19,13 +21,15 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "common.cuh"
 
 namespace {
 
-constexpr int kOut = 256;     // outputs per CTA
 constexpr int kThreads = 256;
+constexpr int kOPT = 4;                  // outputs per thread
+constexpr int kStage = 8192;             // staged samples per CTA at most (64 KB), when kout allows
 
 template <typename S>
 __device__ __forceinline__ float rf_sample(const S* p, int64_t i);
@@ -35,6 +39,27 @@ template <>
 __device__ __forceinline__ float rf_sample<int16_t>(const int16_t* p, int64_t i) { return (float)__ldg(p + i); }
 template <>
 __device__ __forceinline__ float rf_sample<__half>(const __half* p, int64_t i) { return __half2float(__ldg(p + i)); }
+
+// 4 consecutive samples starting at an index whose address is 4-sample aligned
+template <typename S>
+__device__ __forceinline__ float4 rf_vec4(const S* p, int64_t i);
+template <>
+__device__ __forceinline__ float4 rf_vec4<float>(const float* p, int64_t i) {
+    return __ldg(reinterpret_cast<const float4*>(p + i));
+}
+template <>
+__device__ __forceinline__ float4 rf_vec4<int16_t>(const int16_t* p, int64_t i) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(p + i));
+    return make_float4((float)(int16_t)(u.x & 0xFFFF), (float)(int16_t)(u.x >> 16), (float)(int16_t)(u.y & 0xFFFF),
+                       (float)(int16_t)(u.y >> 16));
+}
+template <>
+__device__ __forceinline__ float4 rf_vec4<__half>(const __half* p, int64_t i) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(p + i));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
 
 template <typename D>
 __device__ __forceinline__ void store_iq(D* out, int64_t i, float2 v);
@@ -53,7 +78,7 @@ __device__ __forceinline__ void store_iq<__nv_bfloat16>(__nv_bfloat16* out, int6
 
 struct DemodArgs {
     int64_t L, Ld, n_traces;
-    int D, ntaps;
+    int D, ntaps, kout;  // kout: outputs per CTA (<= kThreads * kOPT)
     float c0;              // fractional part of fc * t0 (cycles)
     float step_hi, step_lo;  // fc / fs split into two floats
     float scale;
@@ -62,52 +87,100 @@ struct DemodArgs {
 template <typename S, typename D>
 __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ rf, D* __restrict__ iq,
                                                          const float* __restrict__ taps, const DemodArgs a) {
-    extern __shared__ float2 mix[];  // [kOut * D + ntaps - 1]
-    const int64_t chunks = (a.Ld + kOut - 1) / kOut;
+    // shared: taps[ntaps], then the mixed samples [kout * D + ntaps - 1]
+    extern __shared__ float2 smem2[];
+    float* tap = reinterpret_cast<float*>(smem2);
+    float2* mix = smem2 + (a.ntaps + 1) / 2;
+    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t trace = blockIdx.x / chunks;
-    const int64_t m0 = (blockIdx.x - trace * chunks) * kOut;
+    const int64_t m0 = (blockIdx.x - trace * chunks) * a.kout;
     if (trace >= a.n_traces) return;
+    for (int k = threadIdx.x; k < a.ntaps; k += kThreads) tap[k] = __ldg(taps + k);
     const S* x = rf + trace * a.L;
-    const int64_t j0 = m0 * a.D - (a.ntaps - 1);  // first staged sample (may be negative)
-    const int nstage = kOut * a.D + a.ntaps - 1;
-    for (int s = threadIdx.x; s < nstage; s += kThreads) {
-        const int64_t j = j0 + s;
-        float2 v = make_float2(0.f, 0.f);
-        if (j >= 0 && j < a.L) {
-            const float jf = (float)j;  // exact: L < 2^24
-            const float p = jf * a.step_hi;
-            const float e = fmaf(jf, a.step_hi, -p);  // rounding error of the product
-            const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
-            float sn, cs;
-            __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
-            const float r = a.scale * rf_sample<S>(x, j);
-            v = make_float2(r * cs, r * sn);
+    // staged window [j0, j0 + nstage), stored from jb <= j0 where the address of
+    // sample jb is 4-sample aligned, so that threads load 4 samples per instruction
+    const int64_t j0 = m0 * a.D - (a.ntaps - 1);  // first needed sample (may be negative)
+    const int off = (int)((((trace * a.L + j0) % 4) + 4) % 4);
+    const int64_t jb = j0 - off;
+    const int nstage = a.kout * a.D + a.ntaps - 1 + off;
+    // the staged samples are stored polyphase: sample s at mix[(s % D) * Q + s / D], so
+    // that for one tap the 32 outputs of a warp read 32 consecutive float2
+    const int Q = (nstage + a.D - 1) / a.D;
+    for (int s0 = 4 * threadIdx.x; s0 < nstage; s0 += 4 * kThreads) {
+        const int64_t jv = jb + s0;
+        float r[4];
+        if (jv >= 0 && jv + 3 < a.L) {
+            const float4 v = rf_vec4<S>(x, jv);
+            r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+        } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) r[u] = (jv + u >= 0 && jv + u < a.L) ? rf_sample<S>(x, jv + u) : 0.f;
         }
-        mix[s] = v;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int s = s0 + u;
+            if (s >= nstage) break;
+            const int64_t j = jv + u;
+            float2 v = make_float2(0.f, 0.f);
+            if (j >= 0 && j < a.L) {
+                const float jf = (float)j;  // exact: L < 2^24
+                const float p = jf * a.step_hi;
+                const float e = fmaf(jf, a.step_hi, -p);  // rounding error of the product
+                const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
+                float sn, cs;
+                __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
+                const float rr = a.scale * r[u];
+                v = make_float2(rr * cs, rr * sn);
+            }
+            mix[(s % a.D) * Q + s / a.D] = v;  // polyphase: phase-major
+        }
     }
     __syncthreads();
-    for (int o = threadIdx.x; o < kOut; o += kThreads) {
-        const int64_t m = m0 + o;
-        if (m >= a.Ld) break;
-        // y[m] = sum_k b[k] mix[m*D - k]; in the staged window m*D - k sits at o*D + ntaps-1 - k
-        const float2* w = mix + (int64_t)o * a.D + a.ntaps - 1;
-        float2 acc = make_float2(0.f, 0.f);
+    // outputs o = threadIdx.x + kThreads * q, kOPT per thread: independent accumulators
+    float2 acc[kOPT];
+#pragma unroll
+    for (int q = 0; q < kOPT; ++q) acc[q] = make_float2(0.f, 0.f);
+    const int last = a.ntaps - 1 + off;
+    // tap k reads staged sample o*D + last - k: phase (last - k) % D, offset (last - k) / D,
+    // stepped down incrementally instead of divided per tap
+    auto fir = [&](auto full) {
+        int ph = last % a.D, qo = last / a.D;
         for (int k = 0; k < a.ntaps; ++k) {
-            const float b = __ldg(taps + k);
-            const float2 v = w[-k];
-            acc.x = fmaf(b, v.x, acc.x);
-            acc.y = fmaf(b, v.y, acc.y);
+            const float b = tap[k];
+            const float2* row = mix + ph * Q + qo;
+#pragma unroll
+            for (int q = 0; q < kOPT; ++q) {
+                const int o = threadIdx.x + kThreads * q;
+                if (decltype(full)::value || o < a.kout) {
+                    const float2 v = row[o];
+                    acc[q].x = fmaf(b, v.x, acc[q].x);
+                    acc[q].y = fmaf(b, v.y, acc[q].y);
+                }
+            }
+            if (ph == 0) {
+                ph = a.D - 1;
+                --qo;
+            } else {
+                --ph;
+            }
         }
-        store_iq<D>(iq, trace * a.Ld + m, acc);
+    };
+    if (a.kout == kThreads * kOPT) fir(std::true_type{});
+    else fir(std::false_type{});
+#pragma unroll
+    for (int q = 0; q < kOPT; ++q) {
+        const int o = threadIdx.x + kThreads * q;
+        const int64_t m = m0 + o;
+        if (o < a.kout && m < a.Ld) store_iq<D>(iq, trace * a.Ld + m, acc[q]);
     }
 }
 
 template <typename S>
 int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, const DemodArgs& a, cudaStream_t s) {
-    const int64_t chunks = (a.Ld + kOut - 1) / kOut;
+    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t blocks = chunks * a.n_traces;
     USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
-    const size_t smem = sizeof(float2) * (size_t)(kOut * a.D + a.ntaps - 1);
+    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + (size_t)(a.kout * a.D + a.ntaps - 1 + 3) + a.D);
     int dev = 0, optin = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -153,6 +226,7 @@ extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32
     a.n_traces = n_traces;
     a.D = decimation;
     a.ntaps = ntaps;
+    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - ntaps) / decimation));
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;

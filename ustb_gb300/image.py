@@ -72,14 +72,18 @@ def scan_convert(data: torch.Tensor, scan: SectorScan, size_x: int = 512, size_z
     d = data.to(torch.complex64 if cplx else torch.float32).reshape(nd * na, -1)
     F = d.shape[1]
     d = d.t().contiguous()  # (F, P): frame-major, depth fastest
-    xs, zs = cartesian_grid(scan, size_x, size_z)
     dev = data.device
-    f32 = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=dev)
-    depth, azim = f32(scan.depth_axis), f32(scan.azimuth_axis)
-    if not (np.all(np.diff(scan.depth_axis) > 0) and np.all(np.diff(scan.azimuth_axis) > 0)):
-        raise ValueError("depth and azimuth axes must increase")
+    key = (str(dev), size_x, size_z)
+    cache = scan.__dict__.setdefault("_scan_convert_cache", {})
+    if key not in cache:  # axes on the device and the Cartesian grid, once per scan
+        if not (np.all(np.diff(scan.depth_axis) > 0) and np.all(np.diff(scan.azimuth_axis) > 0)):
+            raise ValueError("depth and azimuth axes must increase")
+        f32 = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=dev)
+        xs, zs = cartesian_grid(scan, size_x, size_z)
+        cache[key] = (f32(scan.depth_axis), f32(scan.azimuth_axis), xs, zs,
+                      torch.zeros(1, dtype=torch.float32, device=dev))
+    depth, azim, xs, zs, peak = cache[key]
     out = torch.empty((F, size_x, size_z), dtype=torch.float32, device=dev)
-    peak = torch.zeros(1, dtype=torch.float32, device=dev)
     dx = (xs[-1] - xs[0]) / max(size_x - 1, 1)
     dz = (zs[-1] - zs[0]) / max(size_z - 1, 1)
     with torch.cuda.device(dev):
