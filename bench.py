@@ -607,7 +607,9 @@ def profile_post(args, torch):
     image:     the diverging-wave sector image (256 azimuths x 512 depths) -> 512 x 512
                log-compressed Cartesian image (ustb_scan_convert);
     coherence: its 64-channel cube (dimension.transmit) -> phase and generalized
-               coherence factors."""
+               coherence factors;
+    capon:     the same cube -> Capon minimum variance (32-element subarrays, +-1.5
+               wavelengths of depth averaging, 1 % diagonal loading)."""
     from ustb_gb300 import fast, image, postprocess, preprocess, synth
     from ustb_gb300.das import channel_tensor
     from ustb_gb300.enums import Precision
@@ -637,6 +639,17 @@ def profile_post(args, torch):
             img = o["das"][0]
             fn = lambda: image.scan_convert(img, wl.scan)
             out.update(pixels_in=int(img.numel()), pixels_out=512 * 512)
+        elif args.profile == "capon":
+            cube = o["cube"]
+            cd = wl.channel_data
+            rxa = das.receive_apodization.aperture_apodization(cd.probe, wl.scan)
+            apod = torch.from_numpy(np.ascontiguousarray(rxa.T).astype(np.float32)).to(dev)
+            lam = cd.sound_speed / wl.info["f0"]
+            K = postprocess.capon_k_samples(wl.scan.depth_axis, lam, 1.5)
+            nz, nx = wl.scan.depth_axis.size, wl.scan.azimuth_axis.size
+            fn = lambda: postprocess.capon_minimum_variance(cube, apod, nz, nx, L_elements=32, K_samples=K,
+                                                            regCoef=1e-2)
+            out.update(pixels=nz * nx, channels=int(cube.shape[2]), L_elements=32, K_samples=K)
         else:
             cube = o["cube"]
             fn = lambda: (postprocess.phase_coherence_factor(cube), postprocess.generalized_coherence_factor(cube))
@@ -652,7 +665,7 @@ def main_profile(args):
     workload, ``--steps`` launches each after ``--warmup`` warm-up launches each."""
     import torch
 
-    if args.profile in ("demod", "image", "coherence"):
+    if args.profile in ("demod", "image", "coherence", "capon"):
         return profile_post(args, torch)
 
     from ustb_gb300 import fast, geometry, kernels, synth

@@ -345,6 +345,19 @@ int ustb_generalized_coherence(const void* cube, int64_t P, int64_t K, int64_t F
                                void* image, void* stream);
 
 /*
+ * Capon minimum-variance beamforming on a kept cube (+postprocess/capon_minimum_variance.m:117-177),
+ * per pixel of an nz x nx grid (depth fastest), over the M channels (or waves) of
+ * cube [F][M][nz*nx] complex single: spatial smoothing over subarrays of
+ * L = clamp(floor(L_elements/M * active), 1, active - 1) elements spanning the active
+ * aperture (|apodization [M][nz*nx]| > criterion), temporal averaging over
+ * 2*K_samples + 1 depth samples, diagonal loading regularisation/L * trace R,
+ * optional forward-backward averaging; out [F][nz*nx] complex single.  L <= 32.
+ */
+int ustb_capon(const void* cube, const float* apodization, int64_t nz, int64_t nx, int64_t M, int64_t F,
+               float L_elements, int32_t K_samples, float regularisation, float criterion,
+               int32_t forward_backward, void* out, void* stream);
+
+/*
  * FIR filter along depth with delay compensation, for the band-pass step of the
  * simplified-DMAS post-process (+postprocess/simplified_delay_multiply_and_sum.m:170-176):
  * out[c][z] = sum_k taps[k] * in[c][z + delay - k], zero outside [0, nz).

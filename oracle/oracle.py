@@ -21,6 +21,8 @@ What is here:
                      (with tools/weigthed_std.m, weigthed_var.m, weigthed_mean.m) and
                      +postprocess/generalized_coherence_factor.m:66-97 over one
                      dimension.  Parity unpinned (no golden vectors in the reference).
+* ``capon_f64``     — FP64 numpy restatement of capon_minimum_variance_implementation
+                     (+postprocess/capon_minimum_variance.m:117-177).  Parity unpinned.
 * ``scan_convert_f64`` — FP64 numpy restatement of get_image's compression
                      (+uff/beamformed_data.m:300-316) and +tools/scan_convert.m
                      (bilinear interp2 in (azimuth, depth), -inf outside).  Parity
@@ -284,3 +286,49 @@ def generalized_coherence_factor_f64(data, M0=4, axis=1):
     g = np.take(X, idx, axis=axis).sum(axis) / X.sum(axis)
     g[np.isnan(g)] = 0
     return g, g * d.sum(axis)
+
+
+def capon_f64(data_cube, apod, L_elements, K_samples, regCoef, crit=0.16, fb=False):
+    """z [N, E] from data_cube [N (depth), E (lateral), M] and apod [N, E, M], following
+    capon_minimum_variance_implementation line by line (0-based indices)."""
+    d = np.asarray(data_cube, np.complex128)
+    ap = np.asarray(apod, np.float64)
+    N, E, M = d.shape
+    z = np.zeros((N, E), np.complex128)
+    eps = np.finfo(np.float64).eps
+    for e in range(E):
+        rf = d[:, e, :]
+        for k in range(N):
+            if np.sum(np.abs(rf[k]) > eps) == 0:
+                continue
+            idx = np.nonzero(np.abs(ap[k, e]) > crit)[0]
+            Mn = idx.size
+            if Mn < 2:
+                z[k, e] = rf[k].sum()
+                continue
+            Ln = int(np.floor(L_elements / M * Mn))
+            Ln = 1 if Ln < 1 else (Mn - 1 if Ln >= Mn else Ln)
+            if idx[-1] - Ln + 1 < idx[0]:
+                z[k, e] = rf[k].sum()
+                continue
+            if k - K_samples < 0:
+                rows = rf[:k + K_samples + 1]
+            elif k + K_samples > N - 1:
+                rows = rf[k - K_samples:]
+            else:
+                rows = rf[k - K_samples:k + K_samples + 1]
+            R = np.zeros((Ln, Ln), np.complex128)
+            for l in range(idx[0], idx[-1] - Ln + 2):
+                A = rows[:, l:l + Ln]
+                R += A.conj().T @ A
+            R /= (2 * K_samples + 1) * (Mn - Ln + 1)
+            if fb:
+                R = 0.5 * (R + np.rot90(R.conj(), 2))
+            a = np.ones(Ln)
+            Ria = np.linalg.solve(R + np.eye(Ln) * (regCoef / Ln) * np.trace(R), a)
+            w = Ria / (a.conj() @ Ria)
+            acc = 0
+            for j in range(idx[0], idx[-1] - Ln + 2):
+                acc += w.conj() @ rf[k, j:j + Ln].conj()
+            z[k, e] = acc / (Mn - Ln + 1) * Mn
+    return z

@@ -166,3 +166,33 @@ def generalized_coherence_factor(cube: torch.Tensor, M0: int = 4):
         _lib.call("ustb_generalized_coherence", c.data_ptr(), P, K, F, int(M0), out["GCF"].data_ptr(),
                   out["image"].data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
     return out
+
+
+def capon_k_samples(depth_axis: np.ndarray, wavelength: float, K_in_lambda: float) -> int:
+    """K_samples of capon_minimum_variance.m:178-197: the depth sample nearest K_in_lambda
+    wavelengths below the first, made odd (set.K_in_lambda)."""
+    z = np.asarray(depth_axis, np.float64) / wavelength
+    z = z - z[0]
+    samples = int(np.argmin(np.abs(z - K_in_lambda))) + 1  # MATLAB's 1-based index
+    return samples if samples % 2 else samples + 1
+
+
+def capon_minimum_variance(cube: torch.Tensor, apodization: torch.Tensor, nz: int, nx: int, L_elements: float,
+                           K_samples: int, regCoef: float, active_element_criterium: float = 0.16,
+                           doForwardBackward: bool = False) -> torch.Tensor:
+    """Capon MV (+postprocess/capon_minimum_variance.m) over the kept dimension of
+    ``cube`` (ABI (F, W|1, N|1, P) complex, P = nz * nx with depth fastest).
+    ``apodization``: (K, P) weights of that dimension (tx x rx apodization), the
+    activity test ``|apod| > active_element_criterium``.  Returns (F, P) complex64."""
+    c = _cube_fkp(cube)
+    F, K, P = c.shape
+    if P != nz * nx:
+        raise ValueError(f"cube holds {P} pixels, the grid {nz} x {nx}")
+    dev = c.device
+    ap = apodization.to(torch.float32).reshape(K, P).contiguous()
+    out = torch.empty((F, P), dtype=torch.complex64, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call("ustb_capon", c.data_ptr(), ap.data_ptr(), nz, nx, K, F, float(L_elements), int(K_samples),
+                  float(regCoef), float(active_element_criterium), int(bool(doForwardBackward)), out.data_ptr(),
+                  torch.cuda.current_stream(dev).cuda_stream)
+    return out
