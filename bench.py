@@ -510,11 +510,9 @@ def main():
     mst = cuda_time(table_step, args.steps, flush, stream, torch)
     if world > 1:
         torch.distributed.barrier()
-    ms = statistics.mean(ms32)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    from ustb_gb300 import replicas
+
+    ms = replicas.max_over_ranks(statistics.mean(ms32), dev)  # replicas: the slowest rank's step
     value = units * world / (ms * 1e-3) / 1e9
 
     # end to end through the C-ABI: pinned host channel data in, image out, every step
