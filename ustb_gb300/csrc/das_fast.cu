@@ -657,6 +657,9 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
 #pragma unroll
                 for (int c = 0; c < CG; ++c) {
                     const float2 b = B[c];
+                    // a channel whose receive weight is zero for the whole warp adds
+                    // nothing (das_c skips zero-apodization units too)
+                    if (!__any_sync(0xffffffffu, b.x != 0.f || b.y != 0.f)) continue;
 #pragma unroll
                     for (int k = 0; k < KW; ++k) {
                         if (!decltype(full)::value && k >= kw) continue;  // last, partial wave chunk
@@ -723,6 +726,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
             begin_stage(si);
 #pragma unroll
             for (int c = 0; c < CG; ++c) {
+                if (MODE != USTB_DIM_NONE && !__any_sync(0xffffffffu, B[c].x != 0.f || B[c].y != 0.f)) continue;
 #pragma unroll
                 for (int k = 0; k < KW; ++k) {
                     const float2 v = interp(c, k, stx[k] + srx[c]);
