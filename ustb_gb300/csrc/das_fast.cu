@@ -73,6 +73,7 @@ struct Params {
     float* o_sdmas;
     int64_t rx_f, w_f, f_f;
     uint32_t* flags;
+    int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list)
 };
 
 // ---------------------------------------------------------------------------
@@ -356,7 +357,7 @@ __device__ __forceinline__ void zero_slots() {
 
 // Beamform one tile of one frame (the whole CTA participates).
 template <int MODE, bool CPLX, bool EPI>
-__device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
+__device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, int half = -1) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
     constexpr int CG = StageShape<ORDER_A>::CG;
     constexpr int KW = StageShape<ORDER_A>::KW;
@@ -607,12 +608,16 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
     // are copied while stage si is computed.  One barrier per stage: it makes stage
     // si's entries visible to every warp and frees the other buffer (read by stage
     // si - 1) for stage si + 1's copies.
-    if (nstages > 0) issue(0, 0);
+    // half = 0 / 1: this CTA takes the first / second half of the stage list and adds
+    // its partial sum to the (zeroed) output; -1: the whole list, plain stores
+    const int s_lo = (half == 1) ? nstages / 2 : 0;
+    const int s_hi = (half == 0) ? nstages / 2 : nstages;
+    if (s_lo < s_hi) issue(s_lo, 0);
     auto begin_stage = [&](int si) {
         cp_async_wait_all();
         __syncthreads();
-        if (si + 1 < nstages) issue(si + 1, (si + 1) & 1);
-        bufoff = (unsigned)((si & 1) * NS * kSlot * ES);
+        if (si + 1 < s_hi) issue(si + 1, (si + 1 - s_lo) & 1);
+        bufoff = (unsigned)(((si - s_lo) & 1) * NS * kSlot * ES);
     };
     const float2 zero2 = make_float2(0.f, 0.f);
 
@@ -639,7 +644,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
                 }
             }
         };
-        for (int si = 0; si < nstages; ++si) {
+        for (int si = s_lo; si < s_hi; ++si) {
             const int oc = stage_o(si);
             if (oc != cur) {
                 if (cur >= 0) finish_chunk();
@@ -678,7 +683,19 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
         }
         if (cur >= 0) finish_chunk();
         zero_chunks(cur + 1, NC);
-        if (MODE == USTB_DIM_BOTH) store_cube(p + A.f_f * f, CPLX ? cmul(Y, ph) : Y);
+        if (MODE == USTB_DIM_BOTH) {
+            const float2 y = CPLX ? cmul(Y, ph) : Y;
+            if (half < 0) {
+                store_cube(p + A.f_f * f, y);
+            } else if (live && A.cube) {  // two partial sums per pixel: fl(a + b) in either order
+                if constexpr (CPLX) {
+                    atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].x, y.x);
+                    atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].y, y.y);
+                } else {
+                    atomicAdd(&reinterpret_cast<float*>(A.cube)[p + A.f_f * f], y.x);
+                }
+            }
+        }
     } else {
         if (MODE == USTB_DIM_NONE) {  // units outside the active stages are zero
             for (int n = 0; n < N; ++n)
@@ -766,7 +783,10 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f) {
 template <int MODE, bool CPLX, bool EPI>
 __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX>::value)) das_fast_kernel(const Params A) {
     zero_slots<CPLX>();
-    das_tile<MODE, CPLX, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
+    if (MODE == USTB_DIM_BOTH && A.split == 2)
+        das_tile<MODE, CPLX, EPI>(A, (int)(blockIdx.x >> 1), (int64_t)blockIdx.y, (int)(blockIdx.x & 1));
+    else
+        das_tile<MODE, CPLX, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
 }
 
 // Persistent form: one CTA per SM pulls (request, frame, tile) work items from a
@@ -819,8 +839,17 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
                  (long long)A.N, (long long)A.W, smem, optin);
     auto kern = das_fast_kernel<MODE, CPLX, EPI>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((unsigned)n_tiles, (unsigned)F);
-    kern<<<grid, kTile, smem, s>>>(A);
+    // dimension.both with few tiles (under 4 per SM): two CTAs per tile, each over half of
+    // its stages, add their partial sums into the zeroed image, so the last wave of
+    // tiles is half as long.  With many tiles the tail is already short.
+    int sms = 0;
+    USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    Params B = A;
+    B.split = (MODE == USTB_DIM_BOTH && n_tiles * F < 4 * (int64_t)sms) ? 2 : 1;
+    if (B.split == 2 && B.cube)
+        USTB_CUDA(cudaMemsetAsync(B.cube, 0, (size_t)(B.P * F) * (CPLX ? 8 : 4), s));
+    dim3 grid((unsigned)(n_tiles * B.split), (unsigned)F);
+    kern<<<grid, kTile, smem, s>>>(B);
     USTB_CUDA(cudaGetLastError());
     return USTB_OK;
 }
@@ -1032,6 +1061,7 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
     const OutStrides os = out_strides(dimension, P, N, W);
     A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
     A.flags = flags;
+    A.split = 1;
     return USTB_OK;
 }
 

@@ -514,3 +514,50 @@ def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] 
             _lib.call("ustb_das_fast_batch_ws", ctypes.addressof(arr), n, scratch.data_ptr(), workspace.data_ptr(),
                       workspace.numel() * workspace.element_size(), st)
     return scratch
+
+
+class FramePipeline:
+    """Beamform a stream of frames that live in host memory: frame k+1's copy in and
+    frame k-1's copy out overlap frame k's beamforming.
+
+    ``depth`` CUDA streams take frames in turn, each with its own device input
+    buffer; a frame's host->device copy, its ``ustb_das_fast`` call and the copy of
+    its image back to host memory are ordered on its stream.  ``submit`` returns at
+    once; ``synchronize`` waits for every submitted frame."""
+
+    def __init__(self, geom: FastGeometry, ch_shape, ch_dtype, precision: Precision, is_complex: bool,
+                 dimension=Dimension.both, L: Optional[int] = None, depth: int = 2):
+        dev = geom.device
+        self.geom, self.precision, self.is_complex = geom, Precision(precision), bool(is_complex)
+        self.dimension, self.L = int(dimension), L
+        self.streams = [torch.cuda.Stream(dev) for _ in range(depth)]
+        self.inputs = [torch.empty(ch_shape, dtype=ch_dtype, device=dev) for _ in range(depth)]
+        self.flags = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in range(depth)]
+        self.k = 0
+
+    def start(self) -> None:
+        """Order the pipeline after the work already queued on the current stream."""
+        cur = torch.cuda.current_stream(self.geom.device)
+        for s in self.streams:
+            s.wait_stream(cur)
+
+    def submit(self, host_frame: torch.Tensor, host_out: torch.Tensor) -> None:
+        """Queue one frame: ``host_frame`` (pinned, the storage type of ``precision``
+        or complex64 for FP32) in, its image into ``host_out`` (pinned)."""
+        i = self.k % len(self.streams)
+        self.k += 1
+        s, d_in = self.streams[i], self.inputs[i]
+        with torch.cuda.stream(s):
+            d_in.copy_(host_frame, non_blocking=True)
+            o = das_fast(d_in, self.precision, self.is_complex, self.geom, self.dimension, L=self.L,
+                         flags=self.flags[i], check=False)
+            host_out.copy_(o["cube"], non_blocking=True)
+
+    def synchronize(self) -> None:
+        """Make the current stream wait for every submitted frame (stream-ordered)."""
+        cur = torch.cuda.current_stream(self.geom.device)
+        for s in self.streams:
+            cur.wait_stream(s)
+
+    def overflowed(self) -> bool:
+        return any(int(f.item()) & FLAG_WINDOW_OVERFLOW for f in self.flags)
