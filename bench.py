@@ -508,6 +508,17 @@ def main():
         ms32 = cuda_time(fast_step(st32, Precision.fp32), args.steps, flush, stream, torch)
     ms16 = cuda_time(fast_step(st16, Precision.fp16), args.steps, flush, stream, torch)
     mst = cuda_time(table_step, args.steps, flush, stream, torch)
+    # the two halves of a fast-path step, each timed alone: the entries pass and the
+    # beamforming kernel on prebuilt entries
+    ent = fast.build_entries(st32, Precision.fp32, True, N, W, L=L)
+    kern_step = lambda: fast.das_fast(st32, Precision.fp32, True, geom, 3, L=L, flags=flags, check=False,
+                                      entries=ent)
+    entries_step = lambda: fast.build_entries(st32, Precision.fp32, True, N, W, L=L)
+    for fn in (kern_step, entries_step):
+        for _ in range(warm):
+            fn()
+    msk = cuda_time(kern_step, args.steps, flush, stream, torch)
+    mse = cuda_time(entries_step, args.steps, flush, stream, torch)
     if world > 1:
         torch.distributed.barrier()
     from ustb_gb300 import replicas
@@ -553,7 +564,10 @@ def main():
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
-    achieved = FLOP_PER_UNIT_IQ * act / (ms * 1e-3) / 1e12
+    ms_kernel, ms_entries = statistics.mean(msk), statistics.mean(mse)
+    achieved = FLOP_PER_UNIT_IQ * act / (ms_kernel * 1e-3) / 1e12
+    entry_bytes = ch.numel() * ch.element_size() + fast.entry_bytes(L, N, W, F, True)
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     # compulsory bytes of the fast path: channel data, image, pixel xyz, tile map
     h_bytes_alg = (ch.numel() * ch.element_size() + P * F * 8 + P * 12 + geom.tiles.size * 4)
     res = {
@@ -578,8 +592,14 @@ def main():
             "frac": round(achieved / fp32_peak, 4), "traffic": TRAFFIC_FAST_F32_HEADLINE,
             "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch)",
             "algorithmic_bytes": int(h_bytes_alg),
-            "kernel": "das_fast_kernel<both, complex, f32>",
+            "kernel": "das_fast_kernel<both, complex, f32>", "kernel_ms": round(ms_kernel, 4),
+            "timing": "CUDA events around the beamforming kernel alone (ustb_das_fast_entries on prebuilt entries)",
             "flop_per_unit": FLOP_PER_UNIT_IQ, "units_counted": "das_c_active_units (nonzero tx x rx apodization)",
+            "step_frac": round(FLOP_PER_UNIT_IQ * act / (ms * 1e-3) / 1e12 / fp32_peak, 4),
+            "entries_pass": {"ms": round(ms_entries, 4), "bound": "hbm", "algorithmic_bytes": int(entry_bytes),
+                             "achieved_gbs": round(entry_bytes / (ms_entries * 1e-3) / 1e9, 1),
+                             "peak_gbs": hbm_peak,
+                             "frac": round(entry_bytes / (ms_entries * 1e-3) / 1e9 / hbm_peak, 4)},
             "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max:.0f} "
                            "(MEASURED_PEAKS.json has no FP32 figure)",
         },
@@ -588,7 +608,7 @@ def main():
                 "d2h_bytes_per_step": int(h_out[0].numel() * h_out[0].element_size()),
                 "call": "per frame: cudaMemcpyAsync in + ustb_das_fast + cudaMemcpyAsync out (geometry resident), "
                         "two streams so neighbouring frames' copies overlap the beamforming (fast.FramePipeline)"},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,  # per step: build_entries_kernel + das_fast_kernel
         "clocks": clk.summary(),
     }
     if serving is not None:

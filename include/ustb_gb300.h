@@ -238,6 +238,21 @@ int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex, int64_t L
                   int64_t W, int64_t F, const ustb_das_geometry* geometry, int32_t dimension,
                   int32_t epilogue, const ustb_das_outputs* out, uint32_t* flags, void* stream);
 
+/*
+ * The two halves of ustb_das_fast, for callers that beamform the same channel data
+ * more than once (several scans, apodizations or dimension modes on one
+ * acquisition) or that own the working memory: ustb_build_entries writes the FP32
+ * interpolation entries of ch (ustb_entries_bytes bytes, 16-byte aligned, device)
+ * and ustb_das_fast_entries beamforms from them.  Together they give ustb_das_fast's
+ * results.  No reference counterpart (das_c reads the samples directly).
+ */
+int64_t ustb_entries_bytes(int64_t L, int64_t N, int64_t W, int64_t F, int32_t is_complex);
+int ustb_build_entries(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N, int64_t W,
+                       int64_t F, void* entries, void* stream);
+int ustb_das_fast_entries(const void* entries, int32_t is_complex, int64_t L, int64_t N, int64_t W, int64_t F,
+                          const ustb_das_geometry* geometry, int32_t dimension, int32_t epilogue,
+                          const ustb_das_outputs* out, uint32_t* flags, void* stream);
+
 /* One request of a persistent batched launch (host struct; pointers inside as
  * for ustb_das_fast). */
 typedef struct {

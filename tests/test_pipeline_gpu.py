@@ -32,3 +32,20 @@ def test_pipeline_matches_single_calls(cuda_dev):
     assert not pipe.overflowed()
     for o, r in zip(outs, refs):
         assert torch.equal(o, r)
+
+
+def test_prebuilt_entries_give_the_single_call_result(cuda_dev):
+    wl = synth.config_dw_sector(device=cuda_dev, scale=0.25)
+    das = DAS()
+    das.channel_data, das.scan, das.dimension = wl.channel_data, wl.scan, wl.dimension
+    das.receive_apodization = Apodization(window=wl.rx_window, f_number=wl.rx_f_number)
+    geom = das.fast_geometry(cuda_dev)
+    ch = channel_tensor(wl.channel_data.data, cuda_dev)
+    st = fast.convert_channels(ch, Precision.fp16)
+    L, N, W = ch.shape[-1], geom.N, geom.W
+    ref = fast.das_fast(st, Precision.fp16, True, geom, int(wl.dimension), L=L, epilogue=True)
+    ent = fast.build_entries(st, Precision.fp16, True, N, W, L=L)
+    for _ in range(2):  # the entries serve any number of calls
+        got = fast.das_fast(st, Precision.fp16, True, geom, int(wl.dimension), L=L, epilogue=True, entries=ent)
+        for k in ("cube", "das", "cf", "sdmas"):
+            assert torch.equal(got[k], ref[k]), k

@@ -32,6 +32,9 @@ SIGNATURES = {
     "ustb_apply_pixel_phase": (ctypes.c_int, [vp, i64, i64, vp, vp]),
     "ustb_das_fast": (ctypes.c_int, [vp, i32, i32, i64, i64, i64, i64, vp, i32, i32, vp, vp, vp]),
     "ustb_das_fast_batch": (ctypes.c_int, [vp, i32, vp, vp]),
+    "ustb_entries_bytes": (i64, [i64, i64, i64, i64, i32]),
+    "ustb_build_entries": (ctypes.c_int, [vp, i32, i32, i64, i64, i64, i64, vp, vp]),
+    "ustb_das_fast_entries": (ctypes.c_int, [vp, i32, i64, i64, i64, i64, vp, i32, i32, vp, vp, vp]),
     "ustb_das_fast_workspace_bytes": (i64, [vp, i32]),
     "ustb_das_fast_batch_ws": (ctypes.c_int, [vp, i32, vp, vp, i64, vp]),
     "ustb_convert_channels": (ctypes.c_int, [vp, i32, vp, i32, i64, f32, vp]),

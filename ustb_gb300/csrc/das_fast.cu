@@ -1089,6 +1089,43 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     return USTB_OK;
 }
 
+extern "C" int64_t ustb_entries_bytes(int64_t L, int64_t N, int64_t W, int64_t F, int32_t is_complex) {
+    if (L < 0 || N < 0 || W < 0 || F < 0) return 0;
+    return entry_bytes(L, N, W, F, is_complex != 0);
+}
+
+extern "C" int ustb_build_entries(const void* ch, int32_t storage, int32_t is_complex, int64_t L, int64_t N,
+                                  int64_t W, int64_t F, void* entries, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(storage >= 0 && storage <= 2, USTB_E_DTYPE, "unknown storage type %d", (int)storage);
+    USTB_REQUIRE(L >= 0 && N >= 0 && W >= 0 && F >= 0, USTB_E_SHAPE, "negative size");
+    USTB_REQUIRE(L <= INT32_MAX - 256, USTB_E_SHAPE, "L=%lld exceeds the 32-bit sample index", (long long)L);
+    if (L == 0 || N == 0 || W == 0 || F == 0) return USTB_OK;
+    USTB_REQUIRE(ch && entries, USTB_E_ARG, "NULL pointer");
+    USTB_REQUIRE(((uintptr_t)entries & 15) == 0, USTB_E_ARG, "entries must be 16-byte aligned");
+    return fill_entries(ch, storage, is_complex != 0, L, N, W, F, entries, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int ustb_das_fast_entries(const void* entries, int32_t is_complex, int64_t L, int64_t N, int64_t W,
+                                     int64_t F, const ustb_das_geometry* g, int32_t dimension, int32_t epilogue,
+                                     const ustb_das_outputs* out, uint32_t* flags, void* stream) {
+    ustb::clear_error();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    USTB_REQUIRE(flags, USTB_E_ARG, "flags pointer is NULL");
+    USTB_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t), s));
+    Params A;
+    bool empty = false;
+    // make_params validates the request; the storage type is irrelevant for entries
+    int rc = make_params(entries, USTB_STORE_F32, is_complex, L, N, W, F, g, dimension, epilogue, out, flags, s, A,
+                         empty);
+    if (rc || empty) return rc;
+    USTB_REQUIRE(((uintptr_t)entries & 15) == 0, USTB_E_ARG, "entries must be 16-byte aligned");
+    A.entries = entries;
+    const int64_t nt = g->n_tiles;
+    return is_complex ? dispatch_mode<true>(dimension, epilogue, A, nt, F, s)
+                      : dispatch_mode<false>(dimension, 0, A, nt, F, s);
+}
+
 static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
                                int64_t workspace_bytes, void* stream) {
     ustb::clear_error();

@@ -402,13 +402,30 @@ def convert_channels(src: torch.Tensor, precision: Precision, scale: float = 1.0
     return dst
 
 
+def build_entries(ch: torch.Tensor, precision: Precision, is_complex: bool, N: int, W: int, F: int = 1,
+                  L: Optional[int] = None) -> torch.Tensor:
+    """``ustb_build_entries``: the FP32 interpolation entries of channel data in its
+    storage type, as a uint8 device tensor for ``das_fast(..., entries=...)``."""
+    if L is None:
+        L = ch.numel() // ((2 if is_complex else 1) * N * W * F)
+    nbytes = int(_lib.lib().ustb_entries_bytes(L, N, W, F, int(is_complex)))
+    out = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=ch.device)
+    with torch.cuda.device(ch.device):
+        _lib.call("ustb_build_entries", ch.data_ptr(), STORE[Precision(precision)], int(is_complex), L, N, W, F,
+                  out.data_ptr(), torch.cuda.current_stream(ch.device).cuda_stream)
+    return out
+
+
 def das_fast(ch: torch.Tensor, precision: Precision, is_complex: bool, geom: FastGeometry,
              dimension=Dimension.both, F: int = 1, epilogue: bool = False, cube: bool = True,
-             flags: Optional[torch.Tensor] = None, check: bool = True, L: Optional[int] = None):
+             flags: Optional[torch.Tensor] = None, check: bool = True, L: Optional[int] = None,
+             entries: Optional[torch.Tensor] = None):
     """Run ``ustb_das_fast``.  ``ch`` holds [L,N,W,F] samples of the storage type
     (complex: trailing (re, im) pairs).  Returns a dict of output tensors in the ABI
     layout: 'cube' (F, Wk, Nk, P) and, with the epilogue, 'das', 'cf', 'cf_image',
-    'sdmas' of shape (F, P)."""
+    'sdmas' of shape (F, P).  With ``entries`` (from ``build_entries`` of the same
+    data) only the beamforming kernel runs (``ustb_das_fast_entries``); ``ch`` then
+    only supplies the device and, without ``L``, the sample count."""
     dev = ch.device
     P, N, W = geom.P, geom.N, geom.W
     if L is None:
@@ -431,9 +448,14 @@ def das_fast(ch: torch.Tensor, precision: Precision, is_complex: bool, geom: Fas
     if flags is None:
         flags = torch.zeros(1, dtype=torch.int32, device=dev)
     with torch.cuda.device(dev):
-        _lib.call("ustb_das_fast", ch.data_ptr(), STORE[Precision(precision)], int(is_complex), L, N, W, F,
-                  ctypes.byref(geom.c), int(dimension), int(epilogue), ctypes.byref(o), flags.data_ptr(),
-                  torch.cuda.current_stream(dev).cuda_stream)
+        if entries is None:
+            _lib.call("ustb_das_fast", ch.data_ptr(), STORE[Precision(precision)], int(is_complex), L, N, W, F,
+                      ctypes.byref(geom.c), int(dimension), int(epilogue), ctypes.byref(o), flags.data_ptr(),
+                      torch.cuda.current_stream(dev).cuda_stream)
+        else:
+            _lib.call("ustb_das_fast_entries", entries.data_ptr(), int(is_complex), L, N, W, F,
+                      ctypes.byref(geom.c), int(dimension), int(epilogue), ctypes.byref(o), flags.data_ptr(),
+                      torch.cuda.current_stream(dev).cuda_stream)
     if check:
         fl = int(flags.item())
         if fl & FLAG_WINDOW_OVERFLOW:
