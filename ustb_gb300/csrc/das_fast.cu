@@ -274,18 +274,19 @@ template <int ST, bool CPLX>
 __global__ void __launch_bounds__(256) build_entries_kernel(const void* __restrict__ ch,
                                                             void* __restrict__ entries, int64_t L, int64_t Lp,
                                                             int64_t n_traces) {
-    const int64_t total = n_traces * Lp;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t t = e / Lp, i = e - t * Lp;
-        float2 x0 = make_float2(0.f, 0.f), d = make_float2(0.f, 0.f);
-        if (i >= 1 && i < L - 1) {
-            x0 = load_sample<ST, CPLX>(ch, t * L + i);
-            const float2 x1 = load_sample<ST, CPLX>(ch, t * L + i + 1);
-            d = make_float2(x1.x - x0.x, x1.y - x0.y);
+    // CTAs stride over traces, threads over the samples of a trace (no 64-bit divisions)
+    for (int64_t t = blockIdx.x; t < n_traces; t += gridDim.x) {
+        const int64_t in0 = t * L, out0 = t * Lp;
+        for (int i = threadIdx.x; i < (int)Lp; i += blockDim.x) {
+            float2 x0 = make_float2(0.f, 0.f), d = make_float2(0.f, 0.f);
+            if (i >= 1 && i < (int)L - 1) {
+                x0 = load_sample<ST, CPLX>(ch, in0 + i);
+                const float2 x1 = load_sample<ST, CPLX>(ch, in0 + i + 1);
+                d = make_float2(x1.x - x0.x, x1.y - x0.y);
+            }
+            if constexpr (CPLX) reinterpret_cast<float4*>(entries)[out0 + i] = make_float4(x0.x, x0.y, d.x, d.y);
+            else reinterpret_cast<float2*>(entries)[out0 + i] = make_float2(x0.x, d.x);
         }
-        if constexpr (CPLX) reinterpret_cast<float4*>(entries)[e] = make_float4(x0.x, x0.y, d.x, d.y);
-        else reinterpret_cast<float2*>(entries)[e] = make_float2(x0.x, d.x);
     }
 }
 
@@ -943,7 +944,7 @@ int fill_entries(const void* ch, int32_t storage, bool cplx, int64_t L, int64_t 
     USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int64_t traces = N * W * F, total = traces * L;
     if (total == 0) return USTB_OK;
-    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16);
+    const unsigned grid = (unsigned)std::min<int64_t>(traces, (int64_t)sms * 32);
     switch (storage * 2 + (cplx ? 1 : 0)) {
         case USTB_STORE_F32 * 2 + 1: build_entries_kernel<USTB_STORE_F32, true><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
         case USTB_STORE_F16 * 2 + 1: build_entries_kernel<USTB_STORE_F16, true><<<grid, 256, 0, s>>>(ch, dst, L, L, traces); break;
