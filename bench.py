@@ -345,7 +345,7 @@ def hfr_ensemble(device, torch, reps=5, plain_frames=20):
     sub = fast.convert_channels(x[:8].contiguous(), Precision.fp16, scale)
     run = lambda g: fast.das_fast(sub, Precision.fp16, True, g, int(wl.dimension), F=8, L=L)
     key = autotune.shape_key(wl.scan, N, W, L, 8, Precision.fp16, wl.dimension, True, device)
-    choice = autotune.tune(lambda b, o: das.fast_geometry(device, b, o), run, key, scan=wl.scan)
+    choice = autotune.tune(lambda b, o, c: das.fast_geometry(device, b, o, c), run, key, scan=wl.scan)
     del sub
     geom = das.fast_geometry(device, choice.block, choice.order)
     ens = Ensemble(geom, F, L, wl.dimension, Precision.fp16, scale, graph=True)

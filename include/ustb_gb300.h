@@ -50,7 +50,7 @@ enum { USTB_DIM_NONE = 0, USTB_DIM_RECEIVE = 1, USTB_DIM_TRANSMIT = 2, USTB_DIM_
 const char* ustb_last_error(void);
 
 /* ABI version of this library (major*10000 + minor*100 + patch). */
-int ustb_abi_version(void);
+int ustb_abi_version(void); /* 10100: ustb_das_geometry.ctas_per_tile */
 
 /*
  * Plain single-precision DAS on precomputed delay/apodization tables: the
@@ -197,6 +197,9 @@ typedef struct {
     int32_t rx_use_origin;       /* 0: aperture centred under each pixel; 1: at rx_origin (sector scans) */
     float rx_origin[3];
     float cf_threshold;          /* coherence factor: elements with rx apodization > this count in M */
+    int32_t ctas_per_tile;       /* dimension.both, one launch per request: 1 or 2 CTAs per tile (two
+                                    add partial sums over halves of the tile's work); 0 = the library
+                                    picks 2 when there are fewer than 4 tiles per SM */
 } ustb_das_geometry;
 
 /* Outputs of ustb_das_fast (device pointers; unused ones NULL). */

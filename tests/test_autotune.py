@@ -40,7 +40,7 @@ def test_cache_roundtrip_skips_the_search(tmp_path, monkeypatch):
     monkeypatch.setenv("USTB_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
     autotune._store("k", autotune.Choice((16, 32, 1), "scan", 1.5))
     calls = []
-    got = autotune.tune(lambda b, o: calls.append((b, o)), lambda g: None, "k")
+    got = autotune.tune(lambda *a: calls.append(a), lambda g: None, "k")
     assert got.block == (16, 32, 1) and got.order == "scan" and got.ms == 1.5 and not calls
     data = json.load(open(tmp_path / "t.json"))
     assert data["k"]["order"] == "scan"

@@ -49,3 +49,25 @@ def test_prebuilt_entries_give_the_single_call_result(cuda_dev):
         got = fast.das_fast(st, Precision.fp16, True, geom, int(wl.dimension), L=L, epilogue=True, entries=ent)
         for k in ("cube", "das", "cf", "sdmas"):
             assert torch.equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("cplx", [True, False])
+def test_two_ctas_per_tile_match_one(cuda_dev, cplx):
+    """dimension.both with 1 or 2 CTAs per tile: the same sums, added in two parts."""
+    wl = synth.config_iq_cpwc(device=cuda_dev, scale=0.25) if cplx else synth.config_rf_plane_wave(device=cuda_dev,
+                                                                                                   scale=0.5)
+    das = DAS()
+    das.channel_data, das.scan, das.dimension = wl.channel_data, wl.scan, wl.dimension
+    das.receive_apodization = Apodization(window=wl.rx_window, f_number=wl.rx_f_number)
+    ch = channel_tensor(wl.channel_data.data, cuda_dev)
+    st = fast.convert_channels(ch, Precision.fp32)
+    L = ch.shape[-1]
+    outs = {}
+    for c in (1, 2):
+        g = das.fast_geometry(cuda_dev, ctas_per_tile=c)
+        outs[c] = fast.das_fast(st, Precision.fp32, cplx, g, 3, L=L)["cube"]
+    torch.cuda.synchronize()
+    rel = float((outs[1] - outs[2]).abs().norm() / outs[1].abs().norm())
+    assert rel <= 1e-6
+    again = fast.das_fast(st, Precision.fp32, cplx, das.fast_geometry(cuda_dev, ctas_per_tile=2), 3, L=L)["cube"]
+    assert torch.equal(again, outs[2])  # two partial sums: fl(a + b) in either order

@@ -1,13 +1,15 @@
 """Per-shape tuning of the fast path's tile plan, cached in a JSON file.
 
 What is tuned: the pixel block of a 512-pixel tile along the scan's (depth,
-lateral, elevation) axes, and the order in which tiles are handed to the SMs
-(most receive channels first, or scan order).  The block sets each tile's
+lateral, elevation) axes, the order in which tiles are handed to the SMs (most
+receive channels first, or scan order), and for dimension.both the number of CTAs
+per tile (1, or 2 that each take half of the tile's stages and add their partial
+sums).  The block sets each tile's
 delay spans, hence the length of every staged sample window, how many receive
 channels are active somewhere in the tile, and how the 32 pixels of a warp
 spread over shared-memory banks; the order sets the tail of the launch.  The
-stage shape (slots per stage, samples per slot) and the CTA count (one
-512-thread CTA per SM, which the register file allows) are fixed by the kernel.
+stage shape (slots per stage, samples per slot) and the CTAs per SM (one
+512-thread CTA, which the register file allows) are fixed by the kernel.
 
 Each candidate is timed with CUDA events on the caller's data; the fastest is
 stored under a key made of the device name and the request's shape, so later
@@ -39,6 +41,7 @@ class Choice:
     block: Optional[Tuple[int, ...]]  # None: the planner's default
     order: str                        # "cost" | "scan"
     ms: float = float("nan")          # measured time of one call (CUDA events)
+    ctas_per_tile: int = 0            # dimension.both: 1 or 2 CTAs per tile, 0 = library's choice
 
 
 def cache_path() -> str:
@@ -83,10 +86,13 @@ def shape_key(scan: Scan, n_elements: int, n_waves: int, L: int, F: int, precisi
                                      L, F, int(precision), int(dimension), int(bool(is_complex))))
 
 
-def candidates(scan: Scan) -> List[Choice]:
+def candidates(scan: Scan, both: bool = False) -> List[Choice]:
     """The planner's default block plus power-of-two blocks of 512 pixels over the
-    scan's two largest axes, each in both orders."""
+    scan's two largest axes, each in both orders; for dimension.both also the default
+    block with 1 and with 2 CTAs per tile."""
     out = [Choice(None, "cost"), Choice(None, "scan")]
+    if both:
+        out += [Choice(None, "cost", ctas_per_tile=1), Choice(None, "cost", ctas_per_tile=2)]
     g = _grid_shape(scan)
     if g is None:
         return out
@@ -104,25 +110,26 @@ def candidates(scan: Scan) -> List[Choice]:
     return out
 
 
-def tune(make_geometry: Callable[[Optional[Sequence[int]], str], "fast.FastGeometry"],
+def tune(make_geometry: Callable[..., "fast.FastGeometry"],
          run: Callable[["fast.FastGeometry"], None], key: str, reps: int = 3, refresh: bool = False,
-         cands: Optional[List[Choice]] = None, scan: Optional[Scan] = None) -> Choice:
+         cands: Optional[List[Choice]] = None, scan: Optional[Scan] = None, both: bool = False) -> Choice:
     """Return the cached choice for ``key``, or time every candidate and cache the fastest.
 
-    ``make_geometry(block, order)`` builds a ``FastGeometry`` with that plan;
+    ``make_geometry(block, order, ctas_per_tile)`` builds a ``FastGeometry`` with that plan;
     ``run(geometry)`` launches the work to time on the current stream.  Candidates
     whose plan overflows a sample window (the kernel flags it) are skipped."""
     if not refresh:
         hit = _load().get(key)
         if hit is not None:
             b = hit.get("block")
-            return Choice(tuple(b) if b is not None else None, hit.get("order", "cost"), hit.get("ms", float("nan")))
+            return Choice(tuple(b) if b is not None else None, hit.get("order", "cost"), hit.get("ms", float("nan")),
+                          int(hit.get("ctas_per_tile", 0)))
     if cands is None:
-        cands = candidates(scan) if scan is not None else [Choice(None, "cost")]
+        cands = candidates(scan, both) if scan is not None else [Choice(None, "cost")]
     best: Optional[Choice] = None
     for c in cands:
         try:
-            geom = make_geometry(c.block, c.order)
+            geom = make_geometry(c.block, c.order, c.ctas_per_tile)
         except ValueError:
             continue
         try:
@@ -140,7 +147,7 @@ def tune(make_geometry: Callable[[Optional[Sequence[int]], str], "fast.FastGeome
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         if best is None or ms < best.ms:
-            best = Choice(c.block, c.order, ms)
+            best = Choice(c.block, c.order, ms, c.ctas_per_tile)
     if best is None:
         raise RuntimeError("no tile plan candidate ran")
     _store(key, best)

@@ -73,7 +73,7 @@ struct Params {
     float* o_sdmas;
     int64_t rx_f, w_f, f_f;
     uint32_t* flags;
-    int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list)
+    int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list); 0 = auto
 };
 
 // ---------------------------------------------------------------------------
@@ -846,7 +846,8 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
     int sms = 0;
     USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     Params B = A;
-    B.split = (MODE == USTB_DIM_BOTH && n_tiles * F < 4 * (int64_t)sms) ? 2 : 1;
+    if (MODE != USTB_DIM_BOTH) B.split = 1;
+    else if (B.split == 0) B.split = (n_tiles * F < 4 * (int64_t)sms) ? 2 : 1;
     if (B.split == 2 && B.cube)
         USTB_CUDA(cudaMemsetAsync(B.cube, 0, (size_t)(B.P * F) * (CPLX ? 8 : 4), s));
     dim3 grid((unsigned)(n_tiles * B.split), (unsigned)F);
@@ -1062,7 +1063,8 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
     const OutStrides os = out_strides(dimension, P, N, W);
     A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
     A.flags = flags;
-    A.split = 1;
+    USTB_REQUIRE(g->ctas_per_tile >= 0 && g->ctas_per_tile <= 2, USTB_E_ARG, "ctas_per_tile must be 0, 1 or 2");
+    A.split = g->ctas_per_tile;  // 0: chosen at launch
     return USTB_OK;
 }
 

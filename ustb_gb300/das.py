@@ -149,9 +149,10 @@ class DAS:
             raise ValueError("The modulation frequency > 0 but the input data is real. Check inputs.")
         return ch
 
-    def fast_geometry(self, dev, tile_block=None, tile_order: str = "cost") -> "fast.FastGeometry":
-        """Device geometry for the fast engine; ``tile_block`` / ``tile_order`` as chosen
-        by ``autotune`` (default: the planner's own)."""
+    def fast_geometry(self, dev, tile_block=None, tile_order: str = "cost",
+                      ctas_per_tile: int = 0) -> "fast.FastGeometry":
+        """Device geometry for the fast engine; ``tile_block`` / ``tile_order`` /
+        ``ctas_per_tile`` as chosen by ``autotune`` (default: the library's own)."""
         from . import fast
 
         cd = self.channel_data
@@ -162,7 +163,7 @@ class DAS:
                                  self.receive_apodization, self.transmit_apodization,
                                  self.lens_delay, self.spherical_transmit_delay_model,
                                  self.pw_margin, self.blending_power, pixel_phase=ph,
-                                 tile_block=tile_block, tile_order=tile_order)
+                                 tile_block=tile_block, tile_order=tile_order, ctas_per_tile=ctas_per_tile)
 
     def _go_fast(self) -> BeamformedData:
         from . import fast
