@@ -357,6 +357,10 @@ __device__ __forceinline__ void zero_slots() {
 }
 
 // Beamform one tile of one frame (the whole CTA participates).
+__host__ __device__ __forceinline__ size_t tile_hdr_bytes(int64_t N, int64_t W, int64_t NG, int64_t NC) {
+    return 8 * (size_t)(N + W) + 4 * (size_t)(NG * NC) + (size_t)(N + W) + (size_t)(NG + NC);
+}
+
 template <int MODE, bool CPLX, bool EPI>
 __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, int half = -1) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
@@ -380,6 +384,8 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     unsigned char* act_w = act_n + N;
     unsigned char* act_g = act_w + W;  // channel groups
     unsigned char* act_c = act_g + NG; // wave chunks
+    int2* bl_n = reinterpret_cast<int2*>(smem + slot_buffer_bytes<CPLX>() + ((tile_hdr_bytes(N, W, NG, NC) + 15) & ~size_t(15)));
+    int2* bl_w = bl_n + NG * CG;  // {window base, length} per channel / wave; length < 0: no copy
     __shared__ float2 s_red[kTile / 32];
     __shared__ int s_nstages;
 
@@ -449,6 +455,16 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         }
     }
     __syncthreads();
+    for (int i = tid; i < NG * CG + NC * KW; i += kTile) {
+        int2 v = make_int2(0, -(1 << 20));
+        if (i < NG * CG) {
+            if (i < N && act_n[i]) v = make_int2((int)base_n[i], len_n[i]);
+        } else {
+            const int w = i - NG * CG;
+            if (w < W && act_w[w]) v = make_int2((int)base_w[w], len_w[w]);
+        }
+        bl_n[i] = v;
+    }
     for (int g = tid; g < NG; g += kTile) {
         bool a = false;
         for (int c = 0; c < CG; ++c) a |= (g * CG + c < N) && act_n[g * CG + c];
@@ -485,25 +501,32 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     auto stage_w0 = [&](int si) { return (ORDER_A ? stage_o(si) : stage_i(si)) * KW; };
     auto stage_n0 = [&](int si) { return (ORDER_A ? stage_i(si) : stage_o(si)) * CG; };
 
-    // Stage si's windows into buffer `buf`.  Warp v stages slots v and v + 16; its
-    // lanes copy the window [i0, i0 + len) entry by entry with cp.async, and store
-    // zeros for the entries outside the trace.  Slots without work are left as they
-    // are: their units carry zero weight and read finite stale entries.
+    // Stage si's windows into buffer `buf`.  Half-warp h of warp v stages slot
+    // v + 16 h: its 16 lanes copy the window [i0, i0 + len) entry by entry with
+    // cp.async, and store zeros for the entries outside the trace (bounds are
+    // checked only for windows that cross an end of the trace).  i0 and len come
+    // from the packed per-tile {base, length} of the slot's channel and wave; an
+    // inactive channel or wave has a negative length.  Slots without work are left
+    // as they are: their units carry zero weight and read finite stale entries.
     constexpr int NWARPS = kTile / 32;
-    const Entry* ent = reinterpret_cast<const Entry*>(A.entries);
+    const Entry* ent_f = reinterpret_cast<const Entry*>(A.entries) + frame_tr * A.Lp;
+    const int Nn = (int)N;
     auto issue = [&](int si, int buf) {
+        static_assert(NS == 2 * NWARPS, "two slots per warp");
         const int w0 = stage_w0(si), n0 = stage_n0(si);
-#pragma unroll
-        for (int r = 0; r < NS / NWARPS; ++r) {
-            const int sl = warp + NWARPS * r;
-            const int c = sl / KW, k = sl - (sl / KW) * KW;
-            const int n = n0 + c, w = w0 + k;
-            if (!(n < N && w < W && act_n[n] && act_w[w])) continue;
-            const int len = min(kSlot, len_n[n] + len_w[w] + 3);
-            const int i0 = __float2int_rn(base_n[n] + base_w[w]);
-            const Entry* src = ent + (frame_tr + (int64_t)w * N + n) * A.Lp;
-            const uint32_t dst = slots_s + (uint32_t)((buf * NS + sl) * kSlot * ES);
-            for (int j = lane; j < len; j += 32) {
+        const int sl = warp + NWARPS * (lane >> 4);  // half-warp h of warp v: slot v + NWARPS h
+        const int c = sl / KW, k = sl - (sl / KW) * KW;
+        const int n = n0 + c, w = w0 + k;
+        const int2 a = bl_n[n], b = bl_w[w];
+        const int len = min(kSlot, a.y + b.y + 3);
+        const int i0 = a.x + b.x;
+        const Entry* src = ent_f + (int64_t)(w * Nn + n) * A.Lp;
+        const uint32_t dst = slots_s + (uint32_t)((buf * NS + sl) * kSlot * ES);
+        const int hl = lane & 15;
+        if (i0 >= 0 && i0 + len <= Lc) {
+            for (int j = hl; j < len; j += 16) cp_async<ES>(dst + (uint32_t)(j * ES), src + i0 + j);
+        } else {
+            for (int j = hl; j < len; j += 16) {
                 const int i = i0 + j;
                 if ((unsigned)i < (unsigned)Lc) {
                     cp_async<ES>(dst + (uint32_t)(j * ES), src + i);
@@ -825,8 +848,8 @@ size_t smem_bytes(int64_t N, int64_t W) {
     constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
     constexpr int CG = StageShape<ORDER_A>::CG, KW = StageShape<ORDER_A>::KW;
     const size_t NG = (size_t)((N + CG - 1) / CG), NC = (size_t)((W + KW - 1) / KW);
-    const size_t hdr = 8 * (size_t)(N + W) + 4 * NG * NC + (size_t)(N + W) + NG + NC;
-    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15));
+    const size_t hdr = tile_hdr_bytes(N, W, NG, NC);
+    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15)) + 8 * (NG * CG + NC * KW);
 }
 
 template <int MODE, bool CPLX, bool EPI>
