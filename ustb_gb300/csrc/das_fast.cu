@@ -386,6 +386,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     unsigned char* act_c = act_g + NG; // wave chunks
     int2* bl_n = reinterpret_cast<int2*>(smem + slot_buffer_bytes<CPLX>() + ((tile_hdr_bytes(N, W, NG, NC) + 15) & ~size_t(15)));
     int2* bl_w = bl_n + NG * CG;  // {window base, length} per channel / wave; length < 0: no copy
+    float4* el4 = reinterpret_cast<float4*>(bl_w + NC * KW);  // per channel: x, y, z, window base
     __shared__ float2 s_red[kTile / 32];
     __shared__ int s_nstages;
 
@@ -421,6 +422,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         const bool act = rx_active(A, box, ex, ey, ez);
         if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
         base_n[n] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        el4[n] = make_float4(ex, ey, ez, base_n[n]);
         len_n[n] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
         act_n[n] = act ? 1 : 0;
     }
@@ -560,11 +562,12 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
             float s = 0.f, apo = 0.f;
             float2 bb = make_float2(0.f, 0.f);
             if (n < N && act_n[n]) {
-                const float ex = __ldg(A.el + 3 * n), ey = __ldg(A.el + 3 * n + 1), ez = __ldg(A.el + 3 * n + 2);
+                const float4 e4 = el4[n];
+                const float ex = e4.x, ey = e4.y, ez = e4.z;
                 const float dx = px - ex, dy = py - ey, dz = pz - ez;
                 const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-30f);
                 const float r = r2 * rsqrtf(r2);
-                s = (r * A.inv_c + A.lens) * A.fs - base_n[n];
+                s = (r * A.inv_c + A.lens) * A.fs - e4.w;
                 apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + (int64_t)n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
                 if (!live) apo = 0.f;
                 if (CPLX) {
@@ -849,7 +852,7 @@ size_t smem_bytes(int64_t N, int64_t W) {
     constexpr int CG = StageShape<ORDER_A>::CG, KW = StageShape<ORDER_A>::KW;
     const size_t NG = (size_t)((N + CG - 1) / CG), NC = (size_t)((W + KW - 1) / KW);
     const size_t hdr = tile_hdr_bytes(N, W, NG, NC);
-    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15)) + 8 * (NG * CG + NC * KW);
+    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15)) + 8 * (NG * CG + NC * KW) + 16 * ((N + 1) & ~int64_t(1)) + 16;
 }
 
 template <int MODE, bool CPLX, bool EPI>

@@ -84,7 +84,9 @@ def simulate(probe: Probe, sequence: List[Wave], xyz: np.ndarray, amp: np.ndarra
     el = torch.as_tensor(probe.xyz, dtype=torch.float64, device=dev)
     pts = torch.as_tensor(xyz, dtype=torch.float64, device=dev)
     a = torch.as_tensor(amp, dtype=torch.complex128, device=dev)
-    imp_re = torch.zeros(W * N * (L + 1), dtype=torch.float32, device=dev)
+    # impulses summed in FP64: index_add_ on a GPU adds in no fixed order, and FP64 sums
+    # rounded to FP32 make the data the same from run to run
+    imp_re = torch.zeros(W * N * (L + 1), dtype=torch.float64, device=dev)
     imp_im = torch.zeros_like(imp_re)
     rx = torch.cdist(pts, el)  # [S, N] metres
     carrier = 0.0 if rf else fd
@@ -102,8 +104,9 @@ def simulate(probe: Probe, sequence: List[Wave], xyz: np.ndarray, amp: np.ndarra
         base = (w * N + torch.arange(N, device=dev)[None, :]) * (L + 1)
         idx = (base + k0.clamp(0, L - 1).to(torch.int64))
         v = torch.where(ok, val, torch.zeros((), dtype=val.dtype, device=dev))
-        vre = v.real.to(torch.float32)
-        vim = v.imag.to(torch.float32)
+        vre = v.real.to(torch.float32).double()
+        vim = v.imag.to(torch.float32).double()
+        frac = frac.double()
         idx, frac, vre, vim = idx.reshape(-1), frac.reshape(-1), vre.reshape(-1), vim.reshape(-1)
         for i in range(0, idx.numel(), chunk):
             sl = slice(i, i + chunk)
@@ -113,9 +116,9 @@ def simulate(probe: Probe, sequence: List[Wave], xyz: np.ndarray, amp: np.ndarra
             if not rf:
                 imp_im.index_add_(0, ii, vim[sl] * (1 - ff))
                 imp_im.index_add_(0, ii + 1, vim[sl] * ff)
-    imp = imp_re.view(W, N, L + 1)[..., :L]
+    imp = imp_re.view(W, N, L + 1)[..., :L].float()
     if not rf:
-        imp = torch.complex(imp, imp_im.view(W, N, L + 1)[..., :L])
+        imp = torch.complex(imp, imp_im.view(W, N, L + 1)[..., :L].float())
     # pulse (RF) or its envelope (IQ) sampled on the grid
     half = int(math.ceil(3.0 / (BW * f0) * fs))
     tk = torch.arange(-half, half + 1, dtype=torch.float64, device=dev) / fs
