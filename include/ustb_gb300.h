@@ -326,6 +326,19 @@ int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32_t dst_type
                     const float* taps, int32_t ntaps, float scale, void* stream);
 
 /*
+ * Zero-phase RF -> IQ demodulation of the reference's Python port
+ * (python/src/ustb/preprocess/fast_demodulation.py:71-134): mix with
+ * exp(-i 2 pi fc (t0 + j/fs)), filter forward and backward with the taps as scipy's
+ * filtfilt(b, 1, x) does (odd extension by 3 * ntaps samples at each end,
+ * steady-state initial conditions in both passes), then keep every D-th sample from
+ * the first; the initial time stays t0.  Arguments and layouts as ustb_demodulate;
+ * L must exceed 3 * ntaps (filtfilt's padding), else USTB_E_SHAPE.
+ */
+int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* iq, int32_t dst_type, int64_t L,
+                             int64_t n_traces, double fs, double t0, double fc, int32_t decimation,
+                             const float* taps, int32_t ntaps, float scale, void* stream);
+
+/*
  * Headless image formation of a sector-scan result: envelope and compression
  * (+uff/beamformed_data.m:300-316 get_image: 0 = log, 20 log10(|b| / max|b|) with the
  * maximum over all frames; 1 = sqrt(|b|); 2 = |b|), then scan conversion onto a

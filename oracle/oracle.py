@@ -31,6 +31,14 @@ What is here:
                      and decimation of +preprocess/fast_demodulation.m:121-167.
                      Parity unpinned: the reference ships no golden vectors for
                      this step and MATLAB is not available to run it.
+* ``hamming_lowpass_taps`` / ``zero_phase_demodulation_f64`` — FP64 numpy
+                     restatement of the reference's Python port,
+                     python/src/ustb/preprocess/fast_demodulation.py:42-88: Hamming
+                     windowed-sinc low-pass (scipy firwin's method), down-mix,
+                     forward-backward filtering with odd extension and steady-state
+                     initial conditions (scipy filtfilt's method), decimation by
+                     slicing.  Pinned to that code's own outputs
+                     (tests/golden/python_demod.npz).
 
 Array convention: every array is given with its MATLAB logical shape
 (channel data [L, N, W, F], tables [P, W] / [P, N]) and is passed to C in
@@ -221,6 +229,49 @@ def fast_demodulation_f64(rf, fs, t0, fc, taps, decimation):
     mix = np.exp(-1j * 2 * np.pi * float(fc) * t).reshape((-1,) + (1,) * (x.ndim - 1))
     y = lfilter(np.asarray(taps, np.float64), [1.0], x * mix, axis=0)
     return y[::int(decimation)]
+
+
+def hamming_lowpass_taps(numtaps, cutoff, fs):
+    """Windowed-sinc low-pass with a Hamming window, scaled to unit gain at DC: the
+    design scipy's firwin(numtaps, cutoff, fs=fs) makes for the reference's Python
+    port (fast_demodulation.py:57-63)."""
+    n = np.arange(int(numtaps), dtype=np.float64) - (int(numtaps) - 1) / 2.0
+    wc = 2.0 * float(cutoff) / float(fs)  # relative to Nyquist
+    h = wc * np.sinc(wc * n)
+    h *= 0.54 - 0.46 * np.cos(2.0 * np.pi * np.arange(int(numtaps)) / (int(numtaps) - 1))
+    return h / h.sum()
+
+
+def _steady_fir(b, x):
+    """y[n] = sum_k b[k] x[max(n - k, 0)] along axis 0: FIR whose input is held at
+    x[0] before the start (lfilter with zi = lfilter_zi(b, 1) * x[0])."""
+    M = len(b)
+    pad = np.concatenate([np.repeat(x[:1], M - 1, axis=0), x], axis=0)
+    y = np.zeros_like(x)
+    for k in range(M):
+        y += b[k] * pad[M - 1 - k:M - 1 - k + x.shape[0]]
+    return y
+
+
+def zero_phase_demodulation_f64(rf, fs, t0, fc, taps, decimation):
+    """IQ of real RF ``rf`` [L, ...] as the reference's Python port makes it
+    (fast_demodulation.py:47-76): data * exp(-1j 2 pi fc t), then filtfilt(b, 1, .)
+    along time — odd extension by P = 3 len(b) samples at both ends, the FIR run
+    forward and backward, each with the input held at its first value before the
+    start, P samples stripped from both ends — then iq[::D].  Raises ValueError
+    when L <= P, as filtfilt does."""
+    b = np.asarray(taps, np.float64)
+    x = np.asarray(rf, np.float64)
+    L = x.shape[0]
+    P = 3 * len(b)
+    if L <= P:
+        raise ValueError(f"trace of {L} samples is not longer than the padding {P}")
+    t = float(t0) + np.arange(L) / float(fs)
+    mix = x * np.exp(-1j * 2 * np.pi * float(fc) * t).reshape((-1,) + (1,) * (x.ndim - 1))
+    ext = np.concatenate([2 * mix[:1] - mix[P:0:-1], mix, 2 * mix[-1:] - mix[-2:-(P + 2):-1]], axis=0)
+    f = _steady_fir(b, ext)
+    g = _steady_fir(b, f[::-1])[::-1]
+    return g[P:P + L][::int(decimation)]
 
 
 def scan_convert_f64(img, depth_axis, azimuth_axis, xs, zs, compression="log"):

@@ -18,6 +18,12 @@ Fixtures written:
                         for plane-wave, diverging-wave and focused (hybrid)
                         sequences: receive/transmit delays and the beamformed
                         output under its interp1 edge rule.
+* ``python_demod.npz``  RF inputs and the IQ output of the reference's Python
+                        ``ustb.preprocess.FastDemodulation``
+                        (python/src/ustb/preprocess/fast_demodulation.py): default
+                        and explicit decimation, 65-tap and short-trace filters,
+                        and a trace too short for filtfilt's padding (the
+                        reference raises there).
 """
 from __future__ import annotations
 
@@ -200,13 +206,70 @@ def make_python_das(out_path, reference_root):
     np.savez_compressed(out_path, **res)
 
 
+def make_python_demod(out_path, reference_root):
+    """Run the reference's Python FastDemodulation on seeded RF and keep its output."""
+    import types
+
+    sys.path.insert(0, os.path.join(reference_root, "python", "src"))
+    # go() imports pyuff_ustb.objects.uff.Uff (unused); a stub module satisfies it
+    for name in ("pyuff_ustb", "pyuff_ustb.objects", "pyuff_ustb.objects.uff"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["pyuff_ustb.objects.uff"].Uff = object
+    from ustb.preprocess.fast_demodulation import FastDemodulation  # reference package
+
+    rng = np.random.default_rng(17)
+    cases = {
+        # name: (L, N, W, fs, t0, fc, downsample_frequency)
+        "default_dec": (600, 3, 2, 40e6, 2e-6, 5e6, None),
+        "explicit_dec": (517, 2, 1, 50e6, 0.0, 3.5e6, 12e6),
+        "no_dec": (400, 2, 2, 20e6, 1e-6, 4e6, 25e6),
+        "int_like": (300, 4, 1, 31.25e6, 5e-7, 5.2e6, None),
+    }
+    res = {}
+    for name, (L, N, W, fs, t0, fc, fds) in cases.items():
+        t = t0 + np.arange(L) / fs
+        env = np.exp(-((t[:, None, None] - rng.uniform(t[L // 4], t[3 * L // 4], (1, N, W))) * fc / 2) ** 2)
+        rf = env * np.cos(2 * np.pi * fc * t[:, None, None] + rng.uniform(0, 2 * np.pi, (1, N, W)))
+        rf += 0.05 * rng.standard_normal((L, N, W))
+        if name == "int_like":
+            rf = np.round(rf * 2000.0)
+        cd = _CD(rf, _Probe(np.arange(N) * 3e-4), [None] * W, fs, t0, 1540.0, 0.0)
+        cd.pulse = None
+        dm = FastDemodulation()
+        dm.input = cd
+        dm.modulation_frequency = fc
+        dm.downsample_frequency = fds
+        out = dm.go()
+        res[f"{name}/rf"] = rf
+        res[f"{name}/params"] = np.array([fs, t0, fc, -1.0 if fds is None else fds])
+        res[f"{name}/iq"] = np.asarray(out.data)
+        res[f"{name}/fs_out"] = np.float64(out.sampling_frequency)
+        res[f"{name}/t0_out"] = np.float64(out.initial_time)
+    # too short for filtfilt's padding: the reference raises ValueError
+    L = 150
+    cd = _CD(rng.standard_normal((L, 1, 1)), _Probe(np.zeros(1)), [None], 20e6, 0.0, 1540.0, 0.0)
+    cd.pulse = None
+    dm = FastDemodulation()
+    dm.input = cd
+    dm.modulation_frequency = 4e6
+    try:
+        dm.go()
+        raised = 0
+    except ValueError:
+        raised = 1
+    res["short/L"] = np.int64(L)
+    res["short/raises"] = np.int64(raised)
+    np.savez_compressed(out_path, **res)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     a = ap.parse_args()
     make_das_c_cases(os.path.join(HERE, "das_c_cases.npz"))
     make_python_das(os.path.join(HERE, "python_das.npz"), a.reference)
-    for f in ("das_c_cases.npz", "python_das.npz"):
+    make_python_demod(os.path.join(HERE, "python_demod.npz"), a.reference)
+    for f in ("das_c_cases.npz", "python_das.npz", "python_demod.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

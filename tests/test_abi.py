@@ -50,6 +50,9 @@ def test_abi_version_and_error_string(lib_path):
 
     h = _lib.lib()
     assert h.ustb_abi_version() >= 10000
+    # every entry point clears the thread's message first: an empty call succeeds
+    # (no work, no CUDA call) and leaves no message behind
+    assert h.ustb_demodulate(None, 0, None, 0, 16, 0, 1.0, 0.0, 0.0, 1, None, 1, 1.0, None) == 0
     assert h.ustb_last_error() == b""
 
 

@@ -47,3 +47,44 @@ def test_oracle_matches_direct_sum():
             if m - k >= 0:
                 want[mi] += b[k] * mix[m - k]
     assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
+
+
+# ---- the reference's Python port: firwin + filtfilt + slicing ---------------
+GOLDEN = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "python_demod.npz"))
+CASES = ["default_dec", "explicit_dec", "no_dec", "int_like"]
+
+
+def python_port_decimation(fs, fc, fds):
+    return max(1, int(np.floor(fs / (4 * fc)))) if fds < 0 else max(1, int(np.floor(fs / fds)))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_zero_phase_oracle_matches_reference_python_port(name):
+    """The oracle restatement against the output of python/src/ustb/preprocess/
+    fast_demodulation.py itself (complex64, so agreement to its rounding)."""
+    rf = GOLDEN[f"{name}/rf"]
+    fs, t0, fc, fds = GOLDEN[f"{name}/params"]
+    taps = preprocess.python_port_taps(fc, fs, rf.shape[0])
+    assert np.allclose(taps, O.hamming_lowpass_taps(len(taps), 0.5 * fc, fs), rtol=0, atol=1e-15)
+    D = python_port_decimation(fs, fc, fds)
+    got = O.zero_phase_demodulation_f64(rf, fs, t0, fc, taps, D)
+    want = GOLDEN[f"{name}/iq"][..., 0]
+    assert got.shape == want.shape
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-7
+    assert float(GOLDEN[f"{name}/fs_out"]) == fs / D
+    assert float(GOLDEN[f"{name}/t0_out"]) == t0
+
+
+def test_zero_phase_short_trace_raises_like_the_reference():
+    assert int(GOLDEN["short/raises"]) == 1
+    L = int(GOLDEN["short/L"])
+    taps = preprocess.python_port_taps(4e6, 20e6, L)
+    with pytest.raises(ValueError):
+        O.zero_phase_demodulation_f64(np.ones((L, 1)), 20e6, 0.0, 4e6, taps, 1)
+
+
+def test_python_port_taps_lengths():
+    assert len(preprocess.python_port_taps(5e6, 40e6, 600)) == 65
+    assert len(preprocess.python_port_taps(5e6, 40e6, 30)) == 19   # 2 (30 // 3) - 1
+    assert len(preprocess.python_port_taps(5e6, 40e6, 4)) == 3     # at least 3
+    assert len(preprocess.python_port_taps(5e6, 40e6, 7)) == 3     # 2 * 2 - 1

@@ -39,6 +39,7 @@ SIGNATURES = {
     "ustb_das_fast_batch_ws": (ctypes.c_int, [vp, i32, vp, vp, i64, vp]),
     "ustb_convert_channels": (ctypes.c_int, [vp, i32, vp, i32, i64, f32, vp]),
     "ustb_demodulate": (ctypes.c_int, [vp, i32, vp, i32, i64, i64, f64, f64, f64, i32, vp, i32, f32, vp]),
+    "ustb_demodulate_filtfilt": (ctypes.c_int, [vp, i32, vp, i32, i64, i64, f64, f64, f64, i32, vp, i32, f32, vp]),
     "ustb_scan_convert": (ctypes.c_int, [vp, i32, i32, i64, i64, i64, vp, vp, vp, vp, i64, i64, f32, f32, f32, f32,
                                          vp]),
     "ustb_phase_coherence": (ctypes.c_int, [vp, i64, i64, i64, vp, f32, f32, vp, vp, vp, vp]),

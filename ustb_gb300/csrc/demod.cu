@@ -204,6 +204,132 @@ int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, con
     return USTB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Zero-phase variant, python/src/ustb/preprocess/fast_demodulation.py:71-134: the
+// mixed trace is filtered forward and backward with the FIR (scipy filtfilt with its
+// defaults: odd extension by P = 3 * ntaps samples at both ends, steady-state initial
+// conditions in both directions) and then sampled every D-th sample from the first,
+// with t0 unchanged:
+//
+//   E[m] = odd extension of mix, m in [0, L + 2P):
+//          2 mix[0] - mix[P - m]            m < P
+//          mix[m - P]                       P <= m < P + L
+//          2 mix[L-1] - mix[2L + P - 2 - m] m >= P + L
+//   f[n] = sum_k b[k] E[max(n - k, 0)]              (forward, steady state before E[0])
+//   g[n] = sum_k b[k] f[min(n + k, L + 2P - 1)]     (backward, steady state after the end)
+//   y[i] = g[i*D + P]
+//
+// The outputs only need f at n >= P, where n - k >= 2P/3 + 1 > 0, so the forward
+// clamp never applies there.  One CTA forms kout consecutive outputs of one trace: it
+// stages the E window they need, computes f over it into a second shared array,
+// then each thread forms outputs from f.
+struct FiltfiltArgs {
+    int64_t L, Ld, n_traces;
+    int D, ntaps, P, kout;
+    float c0, step_hi, step_lo, scale;
+};
+
+template <typename S>
+__device__ __forceinline__ float2 mixed_sample(const S* x, int64_t j, const FiltfiltArgs& a) {
+    const float jf = (float)j;  // exact: L < 2^24
+    const float p = jf * a.step_hi;
+    const float e = fmaf(jf, a.step_hi, -p);
+    const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
+    float sn, cs;
+    __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
+    const float r = a.scale * rf_sample<S>(x, j);
+    return make_float2(r * cs, r * sn);
+}
+
+template <typename S>
+__device__ __forceinline__ float2 extended_sample(const S* x, int64_t m, const FiltfiltArgs& a) {
+    if (m < a.P) {
+        const float2 e0 = mixed_sample<S>(x, 0, a), v = mixed_sample<S>(x, a.P - m, a);
+        return make_float2(2.f * e0.x - v.x, 2.f * e0.y - v.y);
+    }
+    if (m < a.P + a.L) return mixed_sample<S>(x, m - a.P, a);
+    const float2 e1 = mixed_sample<S>(x, a.L - 1, a), v = mixed_sample<S>(x, 2 * a.L + a.P - 2 - m, a);
+    return make_float2(2.f * e1.x - v.x, 2.f * e1.y - v.y);
+}
+
+template <typename S, typename D>
+__global__ void __launch_bounds__(kThreads) filtfilt_kernel(const S* __restrict__ rf, D* __restrict__ iq,
+                                                            const float* __restrict__ taps, const FiltfiltArgs a) {
+    extern __shared__ float2 smem2[];
+    const int M = a.ntaps;
+    float* tap = reinterpret_cast<float*>(smem2);
+    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
+    const int64_t trace = blockIdx.x / chunks;
+    const int64_t m0 = (blockIdx.x - trace * chunks) * a.kout;
+    if (trace >= a.n_traces) return;
+    const int nout = (int)(a.Ld - m0 < a.kout ? a.Ld - m0 : a.kout);
+    const int64_t Ne = a.L + 2 * a.P;
+    const int64_t flo = m0 * a.D + a.P;                                      // first f needed
+    const int64_t fend = (m0 + nout - 1) * a.D + a.P + M - 1;
+    const int64_t fhi = fend < Ne - 1 ? fend : Ne - 1;  // last f needed
+    const int nF = (int)(fhi - flo + 1), nE = nF + M - 1;
+    const int64_t elo = flo - (M - 1);
+    float2* Es = smem2 + (M + 1) / 2;
+    float2* Fs = Es + nE;
+    for (int k = threadIdx.x; k < M; k += kThreads) tap[k] = __ldg(taps + k);
+    const S* x = rf + trace * a.L;
+    for (int e = threadIdx.x; e < nE; e += kThreads) Es[e] = extended_sample<S>(x, elo + e, a);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nF; q += kThreads) {
+        float2 acc = make_float2(0.f, 0.f);
+        const float2* row = Es + q + (M - 1);
+        for (int k = 0; k < M; ++k) {
+            const float b = tap[k];
+            const float2 v = row[-k];
+            acc.x = fmaf(b, v.x, acc.x);
+            acc.y = fmaf(b, v.y, acc.y);
+        }
+        Fs[q] = acc;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < nout; o += kThreads) {
+        const int64_t n = (m0 + o) * a.D + a.P;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = 0; k < M; ++k) {
+            const float b = tap[k];
+            const float2 v = Fs[(n + k < Ne - 1 ? n + k : Ne - 1) - flo];
+            acc.x = fmaf(b, v.x, acc.x);
+            acc.y = fmaf(b, v.y, acc.y);
+        }
+        store_iq<D>(iq, trace * a.Ld + m0 + o, acc);
+    }
+}
+
+template <typename S>
+int launch_filtfilt(const S* rf, void* iq, int32_t dst_type, const float* taps, const FiltfiltArgs& a, cudaStream_t s) {
+    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
+    const int64_t blocks = chunks * a.n_traces;
+    USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
+    const size_t nF = (size_t)(a.kout - 1) * a.D + a.ntaps;
+    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + 2 * nF + a.ntaps);
+    int dev = 0, optin = 0;
+    USTB_CUDA(cudaGetDevice(&dev));
+    USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "decimation %d with %d taps needs %zu bytes of shared memory",
+                 a.D, a.ntaps, smem);
+    switch (dst_type) {
+        case USTB_STORE_F32:
+            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            filtfilt_kernel<S, float><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (float*)iq, taps, a);
+            break;
+        case USTB_STORE_F16:
+            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            filtfilt_kernel<S, __half><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__half*)iq, taps, a);
+            break;
+        default:
+            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            filtfilt_kernel<S, __nv_bfloat16><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__nv_bfloat16*)iq, taps, a);
+            break;
+    }
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
 }  // namespace
 
 extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32_t dst_type, int64_t L,
@@ -238,5 +364,45 @@ extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32
         case USTB_SRC_F32: return launch_demod<float>((const float*)rf, iq, dst_type, taps, a, s);
         case USTB_SRC_I16: return launch_demod<int16_t>((const int16_t*)rf, iq, dst_type, taps, a, s);
         default: return launch_demod<__half>((const __half*)rf, iq, dst_type, taps, a, s);
+    }
+}
+
+extern "C" int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* iq, int32_t dst_type, int64_t L,
+                                        int64_t n_traces, double fs, double t0, double fc, int32_t decimation,
+                                        const float* taps, int32_t ntaps, float scale, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(src_type >= 0 && src_type <= 2, USTB_E_DTYPE, "unknown source type %d", (int)src_type);
+    USTB_REQUIRE(dst_type >= 0 && dst_type <= 2, USTB_E_DTYPE, "unknown storage type %d", (int)dst_type);
+    USTB_REQUIRE(L >= 0 && n_traces >= 0, USTB_E_SHAPE, "negative size");
+    USTB_REQUIRE(L < (1 << 24), USTB_E_SHAPE, "at most 2^24 samples per trace");
+    USTB_REQUIRE(decimation >= 1 && decimation <= 64, USTB_E_ARG, "decimation must be in [1, 64], got %d",
+                 (int)decimation);
+    USTB_REQUIRE(ntaps >= 1 && ntaps <= 1024, USTB_E_ARG, "ntaps must be in [1, 1024], got %d", (int)ntaps);
+    USTB_REQUIRE(fs > 0.0, USTB_E_ARG, "sampling frequency must be > 0");
+    if (n_traces == 0) return USTB_OK;
+    // scipy filtfilt: the trace must be longer than the padding
+    USTB_REQUIRE(L > 3 * (int64_t)ntaps, USTB_E_SHAPE,
+                 "the trace (%lld samples) must be longer than the padding 3 * ntaps = %d", (long long)L,
+                 3 * (int)ntaps);
+    USTB_REQUIRE(rf && iq && taps, USTB_E_ARG, "NULL pointer");
+    FiltfiltArgs a;
+    a.L = L;
+    a.Ld = (L + decimation - 1) / decimation;
+    a.n_traces = n_traces;
+    a.D = decimation;
+    a.ntaps = ntaps;
+    a.P = 3 * ntaps;
+    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage / 2 - ntaps) / decimation + 1));
+    const double c0 = fc * t0;
+    a.c0 = (float)(c0 - std::floor(c0));
+    const double step = fc / fs;
+    a.step_hi = (float)step;
+    a.step_lo = (float)(step - (double)a.step_hi);
+    a.scale = scale;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (src_type) {
+        case USTB_SRC_F32: return launch_filtfilt<float>((const float*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_I16: return launch_filtfilt<int16_t>((const int16_t*)rf, iq, dst_type, taps, a, s);
+        default: return launch_filtfilt<__half>((const __half*)rf, iq, dst_type, taps, a, s);
     }
 }

@@ -66,10 +66,12 @@ def decimation_factor(fs: float, downsample_frequency: float) -> Tuple[int, floa
 
 
 def demodulate(rf: torch.Tensor, fs: float, t0: float, fc: float, taps: np.ndarray, decimation: int,
-               precision: Precision = Precision.fp32, scale: float = 1.0) -> torch.Tensor:
-    """One pass of ``ustb_demodulate``: real RF (..., L) CUDA tensor (float32, int16 or
-    float16; the last dimension is time) -> IQ (..., ceil(L/D), 2) of the storage type
-    (interleaved re, im), where the leading dimensions are independent traces."""
+               precision: Precision = Precision.fp32, scale: float = 1.0, zero_phase: bool = False) -> torch.Tensor:
+    """One pass of ``ustb_demodulate`` (causal FIR) or, with ``zero_phase``,
+    ``ustb_demodulate_filtfilt`` (forward-backward FIR as scipy's filtfilt): real RF
+    (..., L) CUDA tensor (float32, int16 or float16; the last dimension is time) -> IQ
+    (..., ceil(L/D), 2) of the storage type (interleaved re, im), where the leading
+    dimensions are independent traces."""
     if rf.dtype not in SRC or not rf.is_cuda:
         raise TypeError(f"rf must be a float32 / int16 / float16 CUDA tensor, got {rf.dtype} on {rf.device}")
     rf = rf.contiguous()
@@ -80,7 +82,7 @@ def demodulate(rf: torch.Tensor, fs: float, t0: float, fc: float, taps: np.ndarr
     out = torch.empty(tuple(rf.shape[:-1]) + (Ld, 2), dtype=TORCH_STORE[prec], device=rf.device)
     t = torch.as_tensor(np.asarray(taps, np.float32), device=rf.device)
     with torch.cuda.device(rf.device):
-        _lib.call("ustb_demodulate", rf.data_ptr(), SRC[rf.dtype], out.data_ptr(), STORE[prec], L, n_traces,
+        _lib.call("ustb_demodulate_filtfilt" if zero_phase else "ustb_demodulate", rf.data_ptr(), SRC[rf.dtype], out.data_ptr(), STORE[prec], L, n_traces,
                   float(fs), float(t0), float(fc), int(decimation), t.data_ptr(), t.numel(), float(scale),
                   torch.cuda.current_stream(rf.device).cuda_stream)
     return out
@@ -128,3 +130,69 @@ class FastDemodulation:
         iqc = torch.view_as_complex(iq.contiguous()).permute(3, 2, 1, 0)
         delay = (len(taps) - 1) / 2 / fs
         return ChannelData(iqc, cd.probe, cd.sequence, fs_out, float(cd.initial_time) - delay, cd.sound_speed, fc)
+
+
+def python_port_taps(fc: float, fs: float, L: int, lowpass_frequency_vector=(0.5, 1.0)) -> np.ndarray:
+    """Taps of python/src/ustb/preprocess/fast_demodulation.py:57-63: a Hamming-window
+    low-pass of min(65, 2 (L // 3) - 1) taps (at least 3, odd) with cut-off
+    fc * lowpass_frequency_vector[0], unit gain at DC (scipy ``firwin``)."""
+    from scipy.signal import firwin
+
+    numtaps = min(65, L // 3 * 2 - 1)
+    if numtaps < 3:
+        numtaps = 3
+    if numtaps % 2 == 0:
+        numtaps += 1
+    return firwin(numtaps, fc * float(lowpass_frequency_vector[0]), fs=fs)
+
+
+class ZeroPhaseDemodulation:
+    """The reference's Python ``preprocess.FastDemodulation``
+    (python/src/ustb/preprocess/fast_demodulation.py:14-88) on the GPU: down-mix at the
+    modulation frequency, zero-phase low-pass (scipy ``filtfilt`` of ``python_port_taps``),
+    keep every D-th sample with D = floor(fs / downsample_frequency), or
+    floor(fs / (4 fc)) when ``downsample_frequency`` is unset; the initial time is kept.
+    The modulation frequency defaults to ``input.pulse.center_frequency`` when the
+    input has a pulse, else to ``input.modulation_frequency``.  The whole chain is one
+    kernel pass (``ustb_demodulate_filtfilt``); ``go()`` returns IQ ChannelData whose
+    ``data`` is a complex64 [L', N, W, F] view of device memory."""
+
+    def __init__(self):
+        self.input: Optional[ChannelData] = None
+        self.modulation_frequency: Optional[float] = None
+        self.downsample_frequency: Optional[float] = None
+        self.lowpass_frequency_vector = [0.5, 1.0]
+        self.precision = Precision.fp32
+        self.device = torch.device("cuda", 0)
+
+    def _fc(self) -> float:
+        if self.modulation_frequency is not None:
+            return float(self.modulation_frequency)
+        pulse = getattr(self.input, "pulse", None)
+        if pulse is not None and getattr(pulse, "center_frequency", None) is not None:
+            return float(pulse.center_frequency)
+        return float(self.input.modulation_frequency)
+
+    def go(self) -> ChannelData:
+        cd = self.input
+        fs, fc, t0 = float(cd.sampling_frequency), self._fc(), float(cd.initial_time)
+        data = cd.data if torch.is_tensor(cd.data) else torch.as_tensor(np.asarray(cd.data))
+        data = data.to(self.device)
+        if data.is_complex():
+            raise ValueError("fast demodulation takes real RF channel data")
+        while data.dim() < 4:
+            data = data.unsqueeze(-1)
+        L = int(data.shape[0])
+        taps = python_port_taps(fc, fs, L, self.lowpass_frequency_vector)
+        if self.downsample_frequency is not None:
+            D = max(1, int(np.floor(fs / float(self.downsample_frequency))))
+        else:
+            D = max(1, int(np.floor(fs / (4 * fc))))
+        rf = data.permute(3, 2, 1, 0).contiguous()  # [L,N,W,F] -> ABI (F, W, N, L)
+        if rf.dtype not in SRC:
+            rf = rf.to(torch.float32)
+        iq = demodulate(rf, fs, t0, fc, taps, D, self.precision, zero_phase=True)
+        if self.precision != Precision.fp32:
+            iq = iq.float()
+        iqc = torch.view_as_complex(iq.contiguous()).permute(3, 2, 1, 0)
+        return ChannelData(iqc, cd.probe, cd.sequence, fs / D, t0, cd.sound_speed, fc)
