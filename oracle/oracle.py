@@ -16,6 +16,8 @@ What is here:
 * ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
                      +postprocess/coherence_factor.m:100-135 and of the per-pixel
                      term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
+                     The CF is pinned to the output of the reference's Python
+                     CoherenceFactor (tests/golden/python_cf.npz).
 * ``phase_coherence_factor_f64`` / ``generalized_coherence_factor_f64`` — FP64
                      numpy restatements of +postprocess/phase_coherence_factor.m:64-129
                      (with tools/weigthed_std.m, weigthed_var.m, weigthed_mean.m) and

@@ -24,6 +24,11 @@ Fixtures written:
                         and explicit decimation, 65-tap and short-trace filters,
                         and a trace too short for filtfilt's padding (the
                         reference raises there).
+* ``python_cf.npz``     a seeded channel/wave cube (with an all-zero pixel) and
+                        the coherence factor and CF image of the reference's
+                        Python ``ustb.postprocess.CoherenceFactor``
+                        (python/src/ustb/postprocess/coherence_factor.py) for
+                        dimension receive, transmit and both.
 """
 from __future__ import annotations
 
@@ -262,6 +267,28 @@ def make_python_demod(out_path, reference_root):
     np.savez_compressed(out_path, **res)
 
 
+def make_python_cf(out_path, reference_root):
+    """Run the reference's Python CoherenceFactor on a seeded cube."""
+    sys.path.insert(0, os.path.join(reference_root, "python", "src"))
+    from ustb.beamformed_data import BeamformedData  # reference package
+    from ustb.enums import Dimension
+    from ustb.postprocess.coherence_factor import CoherenceFactor
+
+    rng = np.random.default_rng(23)
+    P, N, W, F = 37, 6, 5, 2
+    cube = (rng.standard_normal((P, N, W, F)) + 1j * rng.standard_normal((P, N, W, F))).astype(np.complex64)
+    cube[:, :, :, 0] += (0.8 * np.exp(1j * rng.uniform(0, 2 * np.pi, (P, 1, 1)))).astype(np.complex64)
+    cube[5] = 0  # a pixel with no signal: CF 0
+    res = {"cube": cube}
+    for name in ("receive", "transmit", "both"):
+        cf = CoherenceFactor()
+        cf.input = BeamformedData(scan=None, data=cube)
+        cf.dimension = getattr(Dimension, name)
+        out = cf.go()
+        res[f"{name}/image"] = np.asarray(out.data)
+    np.savez_compressed(out_path, **res)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -269,7 +296,8 @@ def main():
     make_das_c_cases(os.path.join(HERE, "das_c_cases.npz"))
     make_python_das(os.path.join(HERE, "python_das.npz"), a.reference)
     make_python_demod(os.path.join(HERE, "python_demod.npz"), a.reference)
-    for f in ("das_c_cases.npz", "python_das.npz", "python_demod.npz"):
+    make_python_cf(os.path.join(HERE, "python_cf.npz"), a.reference)
+    for f in ("das_c_cases.npz", "python_das.npz", "python_demod.npz", "python_cf.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -132,3 +132,25 @@ def test_cf_and_sdmas_restatements():
     v = O.sdmas_value(np.array([[4.0, 1.0, -9.0]])[:, :, None])
     # ((2 + 1 - 3)^2 - 14) / 2 = -7
     assert np.allclose(v, -7.0)
+
+
+@pytest.mark.parametrize("dim", ["receive", "transmit", "both"])
+def test_cf_restatement_matches_reference_python_coherence_factor(golden_dir, dim):
+    """oracle.coherence_factor against the image of the reference's Python
+    CoherenceFactor (python/src/ustb/postprocess/coherence_factor.py), whose M is the
+    number of summed channels / waves: the restatement with every unit active."""
+    d = np.load(os.path.join(golden_dir, "python_cf.npz"))
+    cube = d["cube"].astype(np.complex128)
+    P, N, W, F = cube.shape
+    if dim == "receive":
+        s, M = cube, N                                           # sum over channels
+    elif dim == "transmit":
+        s, M = np.swapaxes(cube, 1, 2), W                        # sum over waves
+    else:
+        s, M = cube.reshape((P, N * W, 1, F), order="F"), N * W  # both
+    cf, img = O.coherence_factor(s, np.full(P, M))
+    want = d[f"{dim}/image"]
+    got = img if dim != "transmit" else np.swapaxes(img, 1, 2)
+    got = got.reshape(want.shape, order="F")
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-6
+    assert np.all(got[5] == 0) and np.all(want[5] == 0)  # the silent pixel
