@@ -626,6 +626,9 @@ def profile_post(args, torch):
 
     demod:     20 frames x 11 waves x 128 channels x 3072 int16 RF samples (fs 40 MHz,
                f0 5 MHz) -> IQ at fs/4 in FP16 (ustb_demodulate);
+    demod_zero_phase: the same RF through the Python port's zero-phase demodulation
+               (65 Hamming taps forward and backward, D = floor(fs / 4 f0) = 2;
+               ustb_demodulate_filtfilt);
     image:     the diverging-wave sector image (256 azimuths x 512 depths) -> 512 x 512
                log-compressed Cartesian image (ustb_scan_convert);
     coherence: its 64-channel cube (dimension.transmit) -> phase and generalized
@@ -640,13 +643,22 @@ def profile_post(args, torch):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     out = {"profile": args.profile}
-    if args.profile == "demod":
+    if args.profile in ("demod", "demod_zero_phase"):
         g = torch.Generator(device=dev).manual_seed(7)
         rf = (torch.randn((20, 11, 128, 3072), generator=g, device=dev) * 3000).to(torch.int16)
         fs, fc = 40e6, 5e6
-        taps = preprocess.lowpass_taps(fc, fs)
-        D, _ = preprocess.decimation_factor(fs, 2 * fc)
-        fn = lambda: preprocess.demodulate(rf, fs, 0.0, fc, taps, D, Precision.fp16, 1 / 3000)
+        if args.profile == "demod":
+            taps = preprocess.lowpass_taps(fc, fs)
+            D, _ = preprocess.decimation_factor(fs, 2 * fc)
+            fn = lambda: preprocess.demodulate(rf, fs, 0.0, fc, taps, D, Precision.fp16, 1 / 3000)
+        else:
+            taps = preprocess.python_port_taps(fc, fs, rf.shape[-1])
+            D = max(1, int(np.floor(fs / (4 * fc))))
+            fn = lambda: preprocess.demodulate(rf, fs, 0.0, fc, taps, D, Precision.fp16, 1 / 3000, zero_phase=True)
+            L, M, n_tr = rf.shape[-1], len(taps), rf.numel() // rf.shape[-1]
+            # filtfilt at the kept samples is one FIR with the 2M - 1 taps of b's
+            # autocorrelation: 4 FLOP per tap and kept sample (real tap, complex sample)
+            out.update(flop=int(n_tr * (-(-L // D)) * (2 * M - 1) * 4))
         out.update(samples=int(rf.numel()), ntaps=int(len(taps)), decimation=D,
                    bytes=int(rf.numel() * 2 + (rf.numel() // D) * 4))
     else:
@@ -687,7 +699,7 @@ def main_profile(args):
     workload, ``--steps`` launches each after ``--warmup`` warm-up launches each."""
     import torch
 
-    if args.profile in ("demod", "image", "coherence", "capon"):
+    if args.profile in ("demod", "demod_zero_phase", "image", "coherence", "capon"):
         return profile_post(args, torch)
 
     from ustb_gb300 import fast, geometry, kernels, synth

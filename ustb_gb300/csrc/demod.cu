@@ -16,6 +16,13 @@
 // is formed in cycles as c0 + j*step with step split into two floats and the
 // product's rounding error recovered by an FMA, so the phase stays exact to
 // ~1e-7 cycles over any trace length.
+//
+// The zero-phase variant (ustb_demodulate_filtfilt, the reference's Python port,
+// python/src/ustb/preprocess/fast_demodulation.py:47-76) is the same pass with the
+// taps replaced by the autocorrelation of b (2 ntaps - 1 of them, formed per CTA),
+// the sequence shifted by ntaps - 1 samples so the filter is centred, and the
+// trace odd-extended about its end samples (scipy filtfilt's padding) instead of
+// zero-extended.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -79,12 +86,44 @@ __device__ __forceinline__ void store_iq<__nv_bfloat16>(__nv_bfloat16* out, int6
 struct DemodArgs {
     int64_t L, Ld, n_traces;
     int D, ntaps, kout;  // kout: outputs per CTA (<= kThreads * kOPT)
+    int mb, shift;         // zero-phase: taps of the reference filter, and mb - 1
     float c0;              // fractional part of fc * t0 (cycles)
     float step_hi, step_lo;  // fc / fs split into two floats
     float scale;
 };
 
-template <typename S, typename D>
+// scale * x * exp(-i 2 pi fc (t0 + j/fs)) for raw sample value x at index j
+__device__ __forceinline__ float2 mix_value(float x, int64_t j, const DemodArgs& a) {
+    const float jf = (float)j;  // exact: |j| < 2^24
+    const float p = jf * a.step_hi;
+    const float e = fmaf(jf, a.step_hi, -p);  // rounding error of the product
+    const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
+    float sn, cs;
+    __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
+    const float rr = a.scale * x;
+    return make_float2(rr * cs, rr * sn);
+}
+
+// mixed sample j of the sequence the FIR runs over: the trace with zeros outside it,
+// or (zero-phase) its odd extension about both end samples, zero beyond one reflection
+template <typename S, bool ZP>
+__device__ __forceinline__ float2 edge_value(const S* x, int64_t j, const DemodArgs& a) {
+    if (j >= 0 && j < a.L) return mix_value(rf_sample<S>(x, j), j, a);
+    if (!ZP) return make_float2(0.f, 0.f);
+    int64_t e, r;  // end sample and reflected sample
+    if (j < 0) {
+        e = 0;
+        r = -j;
+    } else {
+        e = a.L - 1;
+        r = 2 * a.L - 2 - j;
+    }
+    if (r < 0 || r >= a.L) return make_float2(0.f, 0.f);
+    const float2 ve = mix_value(rf_sample<S>(x, e), e, a), vr = mix_value(rf_sample<S>(x, r), r, a);
+    return make_float2(2.f * ve.x - vr.x, 2.f * ve.y - vr.y);
+}
+
+template <typename S, typename D, bool ZP>
 __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ rf, D* __restrict__ iq,
                                                          const float* __restrict__ taps, const DemodArgs a) {
     // shared: taps[ntaps], then the mixed samples [kout * D + ntaps - 1]
@@ -95,44 +134,51 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     const int64_t trace = blockIdx.x / chunks;
     const int64_t m0 = (blockIdx.x - trace * chunks) * a.kout;
     if (trace >= a.n_traces) return;
-    for (int k = threadIdx.x; k < a.ntaps; k += kThreads) tap[k] = __ldg(taps + k);
+    if constexpr (ZP) {
+        // the single FIR equal to filtfilt at the kept samples: the autocorrelation
+        // h[t] = sum_j b[j] b[j - t], |t| < mb, staged from b in the sample area
+        float* bt = reinterpret_cast<float*>(mix);
+        for (int k = threadIdx.x; k < a.mb; k += kThreads) bt[k] = __ldg(taps + k);
+        __syncthreads();
+        for (int k = threadIdx.x; k < a.ntaps; k += kThreads) {
+            const int t = k - (a.mb - 1);
+            float h = 0.f;
+            for (int j = max(0, t); j < min(a.mb, a.mb + t); ++j) h = fmaf(bt[j], bt[j - t], h);
+            tap[k] = h;
+        }
+        __syncthreads();
+    } else {
+        for (int k = threadIdx.x; k < a.ntaps; k += kThreads) tap[k] = __ldg(taps + k);
+    }
     const S* x = rf + trace * a.L;
-    // staged window [j0, j0 + nstage), stored from jb <= j0 where the address of
-    // sample jb is 4-sample aligned, so that threads load 4 samples per instruction
+    // staged window [j0, j0 + nstage) of the filtered sequence, whose sample j is
+    // trace sample j + shift, stored from jb <= j0 where the address of trace sample
+    // jb + shift is 4-sample aligned, so that threads load 4 samples per instruction
     const int64_t j0 = m0 * a.D - (a.ntaps - 1);  // first needed sample (may be negative)
-    const int off = (int)((((trace * a.L + j0) % 4) + 4) % 4);
+    const int off = (int)((((trace * a.L + j0 + a.shift) % 4) + 4) % 4);
     const int64_t jb = j0 - off;
     const int nstage = a.kout * a.D + a.ntaps - 1 + off;
     // the staged samples are stored polyphase: sample s at mix[(s % D) * Q + s / D], so
     // that for one tap the 32 outputs of a warp read 32 consecutive float2
     const int Q = (nstage + a.D - 1) / a.D;
     for (int s0 = 4 * threadIdx.x; s0 < nstage; s0 += 4 * kThreads) {
-        const int64_t jv = jb + s0;
-        float r[4];
+        const int64_t jv = jb + s0 + a.shift;  // trace index of staged sample s0
+        float2 v[4];
         if (jv >= 0 && jv + 3 < a.L) {
-            const float4 v = rf_vec4<S>(x, jv);
-            r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+            const float4 q = rf_vec4<S>(x, jv);
+            v[0] = mix_value(q.x, jv, a);
+            v[1] = mix_value(q.y, jv + 1, a);
+            v[2] = mix_value(q.z, jv + 2, a);
+            v[3] = mix_value(q.w, jv + 3, a);
         } else {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) r[u] = (jv + u >= 0 && jv + u < a.L) ? rf_sample<S>(x, jv + u) : 0.f;
+            for (int u = 0; u < 4; ++u) v[u] = edge_value<S, ZP>(x, jv + u, a);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int s = s0 + u;
             if (s >= nstage) break;
-            const int64_t j = jv + u;
-            float2 v = make_float2(0.f, 0.f);
-            if (j >= 0 && j < a.L) {
-                const float jf = (float)j;  // exact: L < 2^24
-                const float p = jf * a.step_hi;
-                const float e = fmaf(jf, a.step_hi, -p);  // rounding error of the product
-                const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
-                float sn, cs;
-                __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
-                const float rr = a.scale * r[u];
-                v = make_float2(rr * cs, rr * sn);
-            }
-            mix[(s % a.D) * Q + s / a.D] = v;  // polyphase: phase-major
+            mix[(s % a.D) * Q + s / a.D] = v[u];  // polyphase: phase-major
         }
     }
     __syncthreads();
@@ -175,7 +221,7 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     }
 }
 
-template <typename S>
+template <typename S, bool ZP>
 int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, const DemodArgs& a, cudaStream_t s) {
     const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t blocks = chunks * a.n_traces;
@@ -188,142 +234,16 @@ int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, con
                  a.D, a.ntaps, smem);
     switch (dst_type) {
         case USTB_STORE_F32:
-            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            demod_kernel<S, float><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (float*)iq, taps, a);
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, float, ZP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, float, ZP><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (float*)iq, taps, a);
             break;
         case USTB_STORE_F16:
-            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            demod_kernel<S, __half><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__half*)iq, taps, a);
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __half, ZP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, __half, ZP><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__half*)iq, taps, a);
             break;
         default:
-            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            demod_kernel<S, __nv_bfloat16><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__nv_bfloat16*)iq, taps, a);
-            break;
-    }
-    USTB_CUDA(cudaGetLastError());
-    return USTB_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Zero-phase variant, python/src/ustb/preprocess/fast_demodulation.py:71-134: the
-// mixed trace is filtered forward and backward with the FIR (scipy filtfilt with its
-// defaults: odd extension by P = 3 * ntaps samples at both ends, steady-state initial
-// conditions in both directions) and then sampled every D-th sample from the first,
-// with t0 unchanged:
-//
-//   E[m] = odd extension of mix, m in [0, L + 2P):
-//          2 mix[0] - mix[P - m]            m < P
-//          mix[m - P]                       P <= m < P + L
-//          2 mix[L-1] - mix[2L + P - 2 - m] m >= P + L
-//   f[n] = sum_k b[k] E[max(n - k, 0)]              (forward, steady state before E[0])
-//   g[n] = sum_k b[k] f[min(n + k, L + 2P - 1)]     (backward, steady state after the end)
-//   y[i] = g[i*D + P]
-//
-// The outputs only need f at n >= P, where n - k >= 2P/3 + 1 > 0, so the forward
-// clamp never applies there.  One CTA forms kout consecutive outputs of one trace: it
-// stages the E window they need, computes f over it into a second shared array,
-// then each thread forms outputs from f.
-struct FiltfiltArgs {
-    int64_t L, Ld, n_traces;
-    int D, ntaps, P, kout;
-    float c0, step_hi, step_lo, scale;
-};
-
-template <typename S>
-__device__ __forceinline__ float2 mixed_sample(const S* x, int64_t j, const FiltfiltArgs& a) {
-    const float jf = (float)j;  // exact: L < 2^24
-    const float p = jf * a.step_hi;
-    const float e = fmaf(jf, a.step_hi, -p);
-    const float cyc = (a.c0 + (p - rintf(p))) + fmaf(jf, a.step_lo, e);
-    float sn, cs;
-    __sincosf(-6.283185307179586f * (cyc - rintf(cyc)), &sn, &cs);
-    const float r = a.scale * rf_sample<S>(x, j);
-    return make_float2(r * cs, r * sn);
-}
-
-template <typename S>
-__device__ __forceinline__ float2 extended_sample(const S* x, int64_t m, const FiltfiltArgs& a) {
-    if (m < a.P) {
-        const float2 e0 = mixed_sample<S>(x, 0, a), v = mixed_sample<S>(x, a.P - m, a);
-        return make_float2(2.f * e0.x - v.x, 2.f * e0.y - v.y);
-    }
-    if (m < a.P + a.L) return mixed_sample<S>(x, m - a.P, a);
-    const float2 e1 = mixed_sample<S>(x, a.L - 1, a), v = mixed_sample<S>(x, 2 * a.L + a.P - 2 - m, a);
-    return make_float2(2.f * e1.x - v.x, 2.f * e1.y - v.y);
-}
-
-template <typename S, typename D>
-__global__ void __launch_bounds__(kThreads) filtfilt_kernel(const S* __restrict__ rf, D* __restrict__ iq,
-                                                            const float* __restrict__ taps, const FiltfiltArgs a) {
-    extern __shared__ float2 smem2[];
-    const int M = a.ntaps;
-    float* tap = reinterpret_cast<float*>(smem2);
-    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
-    const int64_t trace = blockIdx.x / chunks;
-    const int64_t m0 = (blockIdx.x - trace * chunks) * a.kout;
-    if (trace >= a.n_traces) return;
-    const int nout = (int)(a.Ld - m0 < a.kout ? a.Ld - m0 : a.kout);
-    const int64_t Ne = a.L + 2 * a.P;
-    const int64_t flo = m0 * a.D + a.P;                                      // first f needed
-    const int64_t fend = (m0 + nout - 1) * a.D + a.P + M - 1;
-    const int64_t fhi = fend < Ne - 1 ? fend : Ne - 1;  // last f needed
-    const int nF = (int)(fhi - flo + 1), nE = nF + M - 1;
-    const int64_t elo = flo - (M - 1);
-    float2* Es = smem2 + (M + 1) / 2;
-    float2* Fs = Es + nE;
-    for (int k = threadIdx.x; k < M; k += kThreads) tap[k] = __ldg(taps + k);
-    const S* x = rf + trace * a.L;
-    for (int e = threadIdx.x; e < nE; e += kThreads) Es[e] = extended_sample<S>(x, elo + e, a);
-    __syncthreads();
-    for (int q = threadIdx.x; q < nF; q += kThreads) {
-        float2 acc = make_float2(0.f, 0.f);
-        const float2* row = Es + q + (M - 1);
-        for (int k = 0; k < M; ++k) {
-            const float b = tap[k];
-            const float2 v = row[-k];
-            acc.x = fmaf(b, v.x, acc.x);
-            acc.y = fmaf(b, v.y, acc.y);
-        }
-        Fs[q] = acc;
-    }
-    __syncthreads();
-    for (int o = threadIdx.x; o < nout; o += kThreads) {
-        const int64_t n = (m0 + o) * a.D + a.P;
-        float2 acc = make_float2(0.f, 0.f);
-        for (int k = 0; k < M; ++k) {
-            const float b = tap[k];
-            const float2 v = Fs[(n + k < Ne - 1 ? n + k : Ne - 1) - flo];
-            acc.x = fmaf(b, v.x, acc.x);
-            acc.y = fmaf(b, v.y, acc.y);
-        }
-        store_iq<D>(iq, trace * a.Ld + m0 + o, acc);
-    }
-}
-
-template <typename S>
-int launch_filtfilt(const S* rf, void* iq, int32_t dst_type, const float* taps, const FiltfiltArgs& a, cudaStream_t s) {
-    const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
-    const int64_t blocks = chunks * a.n_traces;
-    USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
-    const size_t nF = (size_t)(a.kout - 1) * a.D + a.ntaps;
-    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + 2 * nF + a.ntaps);
-    int dev = 0, optin = 0;
-    USTB_CUDA(cudaGetDevice(&dev));
-    USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "decimation %d with %d taps needs %zu bytes of shared memory",
-                 a.D, a.ntaps, smem);
-    switch (dst_type) {
-        case USTB_STORE_F32:
-            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            filtfilt_kernel<S, float><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (float*)iq, taps, a);
-            break;
-        case USTB_STORE_F16:
-            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            filtfilt_kernel<S, __half><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__half*)iq, taps, a);
-            break;
-        default:
-            USTB_CUDA(cudaFuncSetAttribute(filtfilt_kernel<S, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            filtfilt_kernel<S, __nv_bfloat16><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__nv_bfloat16*)iq, taps, a);
+            USTB_CUDA(cudaFuncSetAttribute(demod_kernel<S, __nv_bfloat16, ZP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            demod_kernel<S, __nv_bfloat16, ZP><<<(unsigned)blocks, kThreads, smem, s>>>(rf, (__nv_bfloat16*)iq, taps, a);
             break;
     }
     USTB_CUDA(cudaGetLastError());
@@ -359,11 +279,13 @@ extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32
     a.step_hi = (float)step;
     a.step_lo = (float)(step - (double)a.step_hi);
     a.scale = scale;
+    a.mb = ntaps;
+    a.shift = 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (src_type) {
-        case USTB_SRC_F32: return launch_demod<float>((const float*)rf, iq, dst_type, taps, a, s);
-        case USTB_SRC_I16: return launch_demod<int16_t>((const int16_t*)rf, iq, dst_type, taps, a, s);
-        default: return launch_demod<__half>((const __half*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_F32: return launch_demod<float, false>((const float*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_I16: return launch_demod<int16_t, false>((const int16_t*)rf, iq, dst_type, taps, a, s);
+        default: return launch_demod<__half, false>((const __half*)rf, iq, dst_type, taps, a, s);
     }
 }
 
@@ -385,14 +307,20 @@ extern "C" int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* 
                  "the trace (%lld samples) must be longer than the padding 3 * ntaps = %d", (long long)L,
                  3 * (int)ntaps);
     USTB_REQUIRE(rf && iq && taps, USTB_E_ARG, "NULL pointer");
-    FiltfiltArgs a;
+    // At every kept sample, filtfilt equals one FIR with the 2 ntaps - 1 taps of b's
+    // autocorrelation applied to the odd-extended mixed trace: the kept outputs only
+    // use forward values at least 2 ntaps + 1 samples into the extension and backward
+    // sums that end at least 2 ntaps samples before its end, so neither pass's
+    // steady-state start is reached.
+    DemodArgs a;
     a.L = L;
     a.Ld = (L + decimation - 1) / decimation;
     a.n_traces = n_traces;
     a.D = decimation;
-    a.ntaps = ntaps;
-    a.P = 3 * ntaps;
-    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage / 2 - ntaps) / decimation + 1));
+    a.ntaps = 2 * ntaps - 1;
+    a.mb = ntaps;
+    a.shift = ntaps - 1;
+    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - a.ntaps) / decimation));
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;
@@ -401,8 +329,8 @@ extern "C" int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* 
     a.scale = scale;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (src_type) {
-        case USTB_SRC_F32: return launch_filtfilt<float>((const float*)rf, iq, dst_type, taps, a, s);
-        case USTB_SRC_I16: return launch_filtfilt<int16_t>((const int16_t*)rf, iq, dst_type, taps, a, s);
-        default: return launch_filtfilt<__half>((const __half*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_F32: return launch_demod<float, true>((const float*)rf, iq, dst_type, taps, a, s);
+        case USTB_SRC_I16: return launch_demod<int16_t, true>((const int16_t*)rf, iq, dst_type, taps, a, s);
+        default: return launch_demod<__half, true>((const __half*)rf, iq, dst_type, taps, a, s);
     }
 }
