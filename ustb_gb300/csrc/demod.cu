@@ -140,11 +140,17 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
         float* bt = reinterpret_cast<float*>(mix);
         for (int k = threadIdx.x; k < a.mb; k += kThreads) bt[k] = __ldg(taps + k);
         __syncthreads();
-        for (int k = threadIdx.x; k < a.ntaps; k += kThreads) {
-            const int t = k - (a.mb - 1);
+        // two neighbouring threads per tap, each summing half of the products
+        for (int i0 = 0; i0 < 2 * a.ntaps; i0 += kThreads) {  // bounds uniform across the CTA
+            const int i = i0 + threadIdx.x, k = i >> 1;
             float h = 0.f;
-            for (int j = max(0, t); j < min(a.mb, a.mb + t); ++j) h = fmaf(bt[j], bt[j - t], h);
-            tap[k] = h;
+            if (k < a.ntaps) {
+                const int t = k - (a.mb - 1);
+                const int lo = max(0, t), hi = min(a.mb, a.mb + t), mid = (lo + hi) >> 1;
+                for (int j = (i & 1) ? mid : lo; j < ((i & 1) ? hi : mid); ++j) h = fmaf(bt[j], bt[j - t], h);
+            }
+            h += __shfl_xor_sync(0xffffffffu, h, 1);
+            if (k < a.ntaps && !(i & 1)) tap[k] = h;
         }
         __syncthreads();
     } else {
@@ -221,6 +227,13 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     }
 }
 
+// outputs per CTA: the trace's Ld outputs split into the fewest chunks of at most kmax,
+// all of the same size (a last, short chunk would leave most of its CTA idle)
+int balanced_chunk(int64_t Ld, int64_t kmax) {
+    const int64_t chunks = (Ld + kmax - 1) / kmax;
+    return (int)((Ld + chunks - 1) / chunks);
+}
+
 template <typename S, bool ZP>
 int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, const DemodArgs& a, cudaStream_t s) {
     const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
@@ -272,7 +285,7 @@ extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32
     a.n_traces = n_traces;
     a.D = decimation;
     a.ntaps = ntaps;
-    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - ntaps) / decimation));
+    a.kout = balanced_chunk(a.Ld, std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - ntaps) / decimation)));
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;
@@ -320,7 +333,7 @@ extern "C" int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* 
     a.ntaps = 2 * ntaps - 1;
     a.mb = ntaps;
     a.shift = ntaps - 1;
-    a.kout = (int)std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - a.ntaps) / decimation));
+    a.kout = balanced_chunk(a.Ld, std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - a.ntaps) / decimation)));
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;
