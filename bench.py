@@ -694,6 +694,33 @@ def profile_post(args, torch):
     print(json.dumps(out), flush=True)
 
 
+def profile_ensemble(args, torch):
+    """--profile ensemble: the persistent batch kernel on a 20-frame slice of the
+    high-frame-rate ensemble (20 frames x 11 plane waves x 128 channels x 1536 int16 I/Q
+    samples, 256 x 512 pixels, dimension both): per run the int16 -> FP16 conversion,
+    the entries pass and one persistent launch over all (frame, tile) items."""
+    from ustb_gb300 import synth
+    from ustb_gb300.ensemble import Ensemble
+    from ustb_gb300.enums import Precision
+
+    dev = torch.device("cuda", 0)
+    wl = synth.config_hfr_ensemble(device=dev, frames=20)
+    das = build_das(wl)
+    x = wl.info["int16"]
+    F, W, N, L, _ = x.shape
+    ens = Ensemble(das.fast_geometry(dev), F, L, wl.dimension, Precision.fp16, wl.info["scale"], graph=False)
+    ens.run(x)
+    fn = lambda: ens.run()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        fn()
+    out = {"profile": "ensemble", "frames": F, "units": int(wl.scan.N_pixels) * N * W * F,
+           "ms": [round(t, 4) for t in cuda_time(fn, args.steps, flush, torch.cuda.current_stream(dev), torch)]}
+    torch.cuda.synchronize()
+    out["window_overflow"] = int(ens.flags())
+    print(json.dumps(out), flush=True)
+
+
 def main_profile(args):
     """A short run for ncu: the fast kernel, then the das_c-exact table kernel, on one
     workload, ``--steps`` launches each after ``--warmup`` warm-up launches each."""
@@ -701,6 +728,8 @@ def main_profile(args):
 
     if args.profile in ("demod", "demod_zero_phase", "image", "coherence", "capon"):
         return profile_post(args, torch)
+    if args.profile == "ensemble":
+        return profile_ensemble(args, torch)
 
     from ustb_gb300 import fast, geometry, kernels, synth
     from ustb_gb300.enums import Precision
