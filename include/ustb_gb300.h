@@ -302,6 +302,69 @@ int64_t ustb_das_fast_workspace_bytes(const ustb_das_request* reqs, int32_t n);
 int ustb_das_fast_batch_ws(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
                            int64_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Resident plans and the continuous-batching server                         */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * A plan keeps one acquisition's geometry on the device -- element and pixel
+ * positions, transmit events, optional tables and the tile map -- with the
+ * request shape, so every later frame of that acquisition needs only its
+ * channel data.  The reference rebuilds its delay and apodization tables on
+ * every go() (+midprocess/das.m:91-209) and copies them with each das_cuda call
+ * (+mex/source/das_cuda.cu:171-216).  A plan is immutable once created: any
+ * number of threads may execute it, or submit it to servers, at the same time.
+ */
+typedef struct ustb_plan_s* ustb_plan;
+
+typedef struct {
+    ustb_das_geometry geometry; /* pointer members are HOST arrays here; ustb_plan_create copies
+                                   them to the device.  tile_pixels may be NULL: the library then
+                                   tiles the pixels itself (over pixel_grid when it is given) */
+    int64_t pixel_grid[3];      /* the pixels' grid, first axis fastest, product n_pixels (e.g.
+                                   {N_z, N_x, N_y} of a linear scan, {N_depth, N_azimuth, 1} of a
+                                   sector scan); {0, 0, 0}: no grid */
+    int64_t L, F;               /* samples per trace, frames per request */
+    int32_t storage;            /* USTB_STORE_* of the channel data */
+    int32_t is_complex;
+    int32_t dimension;          /* USTB_DIM_* */
+    int32_t epilogue;           /* as for ustb_das_fast */
+} ustb_plan_desc;
+
+/* Copy the geometry to the device and plan its tiles.  Synchronous. */
+int ustb_plan_create(const ustb_plan_desc* desc, ustb_plan* plan);
+/* Free a plan's device memory.  No call that uses the plan may still be in flight. */
+int ustb_plan_destroy(ustb_plan plan);
+/* Number of tiles of a plan (negative status on a NULL plan). */
+int64_t ustb_plan_tiles(ustb_plan plan);
+/* ustb_das_fast on the plan's geometry: ch [L,N,W,F] of the plan's storage (device). */
+int ustb_plan_execute(ustb_plan plan, const void* ch, const ustb_das_outputs* out, uint32_t* flags,
+                      void* stream);
+
+/*
+ * Continuous-batching server.  ustb_serve_submit queues one request (a plan, its
+ * device channel data and outputs; both must stay valid until the request is
+ * done) and returns at once with a ticket.  A scheduler thread takes queued
+ * requests in arrival order into batches whose interpolation entries fit
+ * `workspace_budget` bytes (at most `max_batch` requests, at most 40) and launches
+ * each batch as ustb_das_fast_batch_ws on the server's own stream, from a
+ * workspace the server owns; a completion thread waits for each batch and marks
+ * its tickets done.  A request whose entries alone exceed the budget runs in a
+ * batch of its own.  The reference serves no requests: das.m beamforms one call
+ * at a time.
+ */
+typedef struct ustb_server_s* ustb_server;
+
+int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, ustb_server* server);
+int ustb_serve_submit(ustb_server server, ustb_plan plan, const void* ch, const ustb_das_outputs* out,
+                      uint64_t* ticket);
+/* Wait until the ticket's request is done (timeout_ms < 0: no limit); USTB_E_TIMEOUT
+ * if it is not done in time (the ticket stays valid), else the request's status,
+ * with its USTB_FLAG_* bits in *flags (may be NULL).  A finished ticket is released. */
+int ustb_serve_wait(ustb_server server, uint64_t ticket, int32_t timeout_ms, uint32_t* flags);
+/* Finish every queued request, stop the threads and free the server. */
+int ustb_serve_destroy(ustb_server server);
+
 /*
  * Convert channel data to a device storage type: count scalars from `src`
  * (USTB_SRC_*) times `scale` into `dst` (USTB_STORE_*), e.g. int16 I/Q scanner

@@ -67,3 +67,57 @@ def test_argument_errors_without_gpu(lib_path):
     rc = h.ustb_das_table_f32(None, 0, 4, 2, 1, 1, 1.0, 0.0, None, None, None, None, 3, 5e6, 3,
                               None, None)
     assert rc == 3 and b"real" in h.ustb_last_error()
+
+
+def test_plan_and_server_argument_errors_without_gpu(lib_path):
+    """NULL handles and descriptors are rejected before any CUDA call."""
+    import ctypes
+
+    from ustb_gb300 import _lib
+
+    h = _lib.lib()
+    assert h.ustb_plan_create(None, None) == 1
+    assert h.ustb_plan_destroy(None) == 1
+    assert h.ustb_plan_tiles(None) == -1
+    assert h.ustb_plan_execute(None, None, None, None, None) == 1
+    assert h.ustb_serve_create(0, 1, None) == 1
+    out = ctypes.c_void_p()
+    assert h.ustb_serve_create(0, 1, ctypes.byref(out)) == 1 and b"budget" in h.ustb_last_error()
+    assert h.ustb_serve_create(1 << 20, 41, ctypes.byref(out)) == 1 and b"max_batch" in h.ustb_last_error()
+    assert h.ustb_serve_submit(None, None, None, None, None) == 1
+    assert h.ustb_serve_wait(None, 1, 0, None) == 1
+    assert h.ustb_serve_destroy(None) == 1
+
+
+def test_plan_descriptor_checks_without_gpu(lib_path):
+    import ctypes
+
+    import numpy as np
+
+    from ustb_gb300 import _lib
+    from ustb_gb300.fast import CWave
+    from ustb_gb300.plan import CPlanDesc
+
+    h = _lib.lib()
+    el = np.zeros((4, 3), np.float32)
+    px = np.zeros((6, 3), np.float32)
+    waves = (CWave * 1)()
+    d = CPlanDesc()
+    d.geometry.n_elements, d.geometry.element_xyz = 4, el.ctypes.data
+    d.geometry.n_pixels, d.geometry.pixel_xyz = 6, px.ctypes.data
+    d.geometry.n_waves, d.geometry.waves = 1, ctypes.addressof(waves)
+    d.geometry.fs, d.geometry.sound_speed = 20e6, 1540.0
+    d.L, d.F, d.dimension, d.is_complex = 64, 1, 3, 1
+    out = ctypes.c_void_p()
+    d.pixel_grid[0], d.pixel_grid[1], d.pixel_grid[2] = 2, 2, 2  # 8 != 6 pixels
+    assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 2 and b"pixel_grid" in h.ustb_last_error()
+    d.pixel_grid[0], d.pixel_grid[1], d.pixel_grid[2] = 3, 2, 1
+    d.L = 1
+    assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 2
+    d.L, d.is_complex, d.geometry.fd = 64, 0, 5e6  # real data with a modulation frequency
+    assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 3
+    d.geometry.fd, d.epilogue, d.dimension = 0.0, 1, 3  # epilogue needs complex transmit mode
+    assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 1
+    d.epilogue = 0
+    waves[0].kind = 3  # table wave without a table
+    assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 1 and b"tx_delay_table" in h.ustb_last_error()

@@ -38,6 +38,14 @@ SIGNATURES = {
     "ustb_das_fast_workspace_bytes": (i64, [vp, i32]),
     "ustb_das_fast_batch_ws": (ctypes.c_int, [vp, i32, vp, vp, i64, vp]),
     "ustb_convert_channels": (ctypes.c_int, [vp, i32, vp, i32, i64, f32, vp]),
+    "ustb_plan_create": (ctypes.c_int, [vp, vp]),
+    "ustb_plan_destroy": (ctypes.c_int, [vp]),
+    "ustb_plan_tiles": (i64, [vp]),
+    "ustb_plan_execute": (ctypes.c_int, [vp, vp, vp, vp, vp]),
+    "ustb_serve_create": (ctypes.c_int, [i64, i32, vp]),
+    "ustb_serve_submit": (ctypes.c_int, [vp, vp, vp, vp, vp]),
+    "ustb_serve_wait": (ctypes.c_int, [vp, ctypes.c_uint64, i32, vp]),
+    "ustb_serve_destroy": (ctypes.c_int, [vp]),
     "ustb_demodulate": (ctypes.c_int, [vp, i32, vp, i32, i64, i64, f64, f64, f64, i32, vp, i32, f32, vp]),
     "ustb_demodulate_filtfilt": (ctypes.c_int, [vp, i32, vp, i32, i64, i64, f64, f64, f64, i32, vp, i32, f32, vp]),
     "ustb_scan_convert": (ctypes.c_int, [vp, i32, i32, i64, i64, i64, vp, vp, vp, vp, i64, i64, f32, f32, f32, f32,

@@ -1,0 +1,265 @@
+// Continuous-batching server over resident plans.
+//
+// Requests are queued by ustb_serve_submit (any thread).  A scheduler thread takes
+// them in arrival order into batches whose interpolation entries fit the workspace
+// budget (at most max_batch requests), launches each batch with
+// ustb_das_fast_batch_ws on the server's stream from the server's workspace, copies
+// the batch's flag word to pinned host memory and records an event.  A completion
+// thread waits for the events in launch order and marks the batches' tickets done.
+// Batches run back to back on one stream, so one workspace serves every batch: a
+// batch's entries pass only starts once the previous batch's kernels are done.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ustb {
+void plan_request(ustb_plan plan, const void* ch, const ustb_das_outputs* out, ustb_das_request* r);
+}
+
+namespace {
+
+constexpr int kMaxBatchRequests = 40;  // the persistent kernel's request table
+constexpr int kFlagSlots = 64;         // pinned flag words (batches in flight at most)
+
+struct Job {
+    uint64_t ticket;
+    ustb_plan plan;
+    const void* ch;
+    ustb_das_outputs out;
+};
+
+struct Done {
+    int status;  // USTB_OK or an error code
+    uint32_t flags;
+    std::string message;
+};
+
+struct Batch {
+    std::vector<uint64_t> tickets;
+    cudaEvent_t ev = nullptr;
+    int slot = -1;   // pinned flag word
+    int status = USTB_OK;
+    std::string message;
+};
+
+}  // namespace
+
+struct ustb_server_s {
+    std::mutex m;
+    std::condition_variable cv_queue, cv_flight, cv_done;
+    std::deque<Job> queue;
+    std::deque<Batch> flight;
+    std::unordered_map<uint64_t, Done> done;
+    std::unordered_set<uint64_t> live;  // submitted and not yet released by a wait
+    uint64_t next_ticket = 1;
+    bool stop = false;           // destroy requested: finish the queue, then exit
+    bool sched_exited = false;   // the scheduler has launched everything it will
+    int64_t budget = 0;
+    int max_batch = 1;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* workspace = nullptr;
+    int64_t ws_bytes = 0;
+    uint64_t* scratch = nullptr;  // device: flag word + queue counters
+    uint64_t* host_flags = nullptr;  // pinned [kFlagSlots]
+    std::vector<int> free_slots;
+    std::thread scheduler, completer;
+
+    void schedule();
+    void complete();
+    int launch(const std::vector<Job>& jobs, Batch& b);
+};
+
+int ustb_server_s::launch(const std::vector<Job>& jobs, Batch& b) {
+    std::vector<ustb_das_request> reqs(jobs.size());
+    for (size_t i = 0; i < jobs.size(); ++i) ustb::plan_request(jobs[i].plan, jobs[i].ch, &jobs[i].out, &reqs[i]);
+    const int64_t need = ustb_das_fast_workspace_bytes(reqs.data(), (int32_t)reqs.size());
+    if (need < 0) return (int)-need;
+    if (need > ws_bytes) {  // grow: the stream must be idle before the old block goes
+        USTB_CUDA(cudaStreamSynchronize(stream));
+        if (workspace) USTB_CUDA(cudaFree(workspace));
+        workspace = nullptr;
+        ws_bytes = 0;
+        USTB_CUDA(cudaMalloc(&workspace, (size_t)need));
+        ws_bytes = need;
+    }
+    const int rc = ustb_das_fast_batch_ws(reqs.data(), (int32_t)reqs.size(), scratch, workspace, ws_bytes, stream);
+    if (rc != USTB_OK) return rc;
+    USTB_CUDA(cudaMemcpyAsync(host_flags + b.slot, scratch, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+    USTB_CUDA(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming | cudaEventBlockingSync));
+    USTB_CUDA(cudaEventRecord(b.ev, stream));
+    return USTB_OK;
+}
+
+void ustb_server_s::schedule() {
+    cudaSetDevice(device);
+    for (;;) {
+        std::vector<Job> jobs;
+        int slot = -1;
+        {
+            std::unique_lock<std::mutex> lk(m);
+            cv_queue.wait(lk, [&] { return stop || !queue.empty(); });
+            if (queue.empty()) break;  // stop requested and nothing left
+            cv_flight.wait(lk, [&] { return !free_slots.empty(); });
+            slot = free_slots.back();
+            free_slots.pop_back();
+            // arrival order; add requests while their entries fit the budget
+            int64_t bytes = 0;
+            while (!queue.empty() && (int)jobs.size() < max_batch) {
+                ustb_das_request r;
+                ustb::plan_request(queue.front().plan, queue.front().ch, &queue.front().out, &r);
+                const int64_t b = ustb_das_fast_workspace_bytes(&r, 1);
+                if (!jobs.empty() && bytes + b > budget) break;
+                bytes += b;
+                jobs.push_back(queue.front());
+                queue.pop_front();
+            }
+        }
+        Batch b;
+        b.slot = slot;
+        for (const Job& j : jobs) b.tickets.push_back(j.ticket);
+        b.status = launch(jobs, b);
+        if (b.status != USTB_OK) b.message = ustb_last_error();
+        {
+            std::lock_guard<std::mutex> lk(m);
+            flight.push_back(std::move(b));
+        }
+        cv_flight.notify_all();
+    }
+    {
+        std::lock_guard<std::mutex> lk(m);
+        sched_exited = true;
+    }
+    cv_flight.notify_all();
+}
+
+void ustb_server_s::complete() {
+    cudaSetDevice(device);
+    for (;;) {
+        Batch b;
+        {
+            std::unique_lock<std::mutex> lk(m);
+            cv_flight.wait(lk, [&] { return !flight.empty() || sched_exited; });
+            if (flight.empty()) break;
+            b = std::move(flight.front());
+            flight.pop_front();
+        }
+        uint32_t flags = 0;
+        if (b.status == USTB_OK) {
+            const cudaError_t e = cudaEventSynchronize(b.ev);
+            if (e != cudaSuccess) {
+                b.status = USTB_E_CUDA;
+                b.message = std::string("batch failed on the device: ") + cudaGetErrorString(e);
+            } else {
+                flags = (uint32_t)(host_flags[b.slot] & 0xffffffffu);
+            }
+        }
+        if (b.ev) cudaEventDestroy(b.ev);
+        {
+            std::lock_guard<std::mutex> lk(m);
+            for (uint64_t t : b.tickets) done[t] = Done{b.status, flags, b.message};
+            free_slots.push_back(b.slot);
+        }
+        cv_done.notify_all();
+        cv_flight.notify_all();
+    }
+}
+
+extern "C" int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, ustb_server* out) {
+    ustb::clear_error();
+    USTB_REQUIRE(out, USTB_E_ARG, "NULL pointer");
+    *out = nullptr;
+    USTB_REQUIRE(workspace_budget > 0, USTB_E_ARG, "workspace budget must be > 0");
+    USTB_REQUIRE(max_batch >= 1 && max_batch <= kMaxBatchRequests, USTB_E_ARG, "max_batch must be in [1, %d]",
+                 kMaxBatchRequests);
+    std::unique_ptr<ustb_server_s> s(new ustb_server_s());
+    s->budget = workspace_budget;
+    s->max_batch = max_batch;
+    USTB_CUDA(cudaGetDevice(&s->device));
+    USTB_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    USTB_CUDA(cudaMalloc(&s->scratch, sizeof(uint64_t) * (kMaxBatchRequests + 1)));
+    USTB_CUDA(cudaHostAlloc(&s->host_flags, sizeof(uint64_t) * kFlagSlots, cudaHostAllocDefault));
+    for (int i = kFlagSlots - 1; i >= 0; --i) s->free_slots.push_back(i);
+    ustb_server_s* raw = s.get();
+    raw->scheduler = std::thread([raw] { raw->schedule(); });
+    raw->completer = std::thread([raw] { raw->complete(); });
+    *out = s.release();
+    return USTB_OK;
+}
+
+extern "C" int ustb_serve_submit(ustb_server s, ustb_plan plan, const void* ch, const ustb_das_outputs* out,
+                                 uint64_t* ticket) {
+    ustb::clear_error();
+    USTB_REQUIRE(s && plan && ch && out && ticket, USTB_E_ARG, "NULL pointer");
+    ustb_das_request r;
+    ustb::plan_request(plan, ch, out, &r);
+    const int64_t need = ustb_das_fast_workspace_bytes(&r, 1);
+    USTB_REQUIRE(need >= 0, (int)-need, "%s", ustb_last_error());
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        USTB_REQUIRE(!s->stop, USTB_E_BUSY, "the server is shutting down");
+        *ticket = s->next_ticket++;
+        s->live.insert(*ticket);
+        s->queue.push_back(Job{*ticket, plan, ch, *out});
+    }
+    s->cv_queue.notify_one();
+    return USTB_OK;
+}
+
+extern "C" int ustb_serve_wait(ustb_server s, uint64_t ticket, int32_t timeout_ms, uint32_t* flags) {
+    ustb::clear_error();
+    USTB_REQUIRE(s, USTB_E_ARG, "NULL server");
+    std::unique_lock<std::mutex> lk(s->m);
+    USTB_REQUIRE(s->live.count(ticket), USTB_E_ARG, "unknown or released ticket %llu", (unsigned long long)ticket);
+    // done, or released meanwhile by another waiter
+    auto ready = [&] { return s->done.count(ticket) != 0 || !s->live.count(ticket); };
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, ready);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+        ustb::set_error("ticket %llu not done after %d ms", (unsigned long long)ticket, (int)timeout_ms);
+        return USTB_E_TIMEOUT;
+    }
+    USTB_REQUIRE(s->live.count(ticket), USTB_E_ARG, "ticket %llu was released by another waiter",
+                 (unsigned long long)ticket);
+    const Done d = s->done[ticket];
+    s->done.erase(ticket);
+    s->live.erase(ticket);
+    if (flags) *flags = d.flags;
+    if (d.status != USTB_OK) ustb::set_error("%s", d.message.c_str());
+    return d.status;
+}
+
+extern "C" int ustb_serve_destroy(ustb_server s) {
+    ustb::clear_error();
+    USTB_REQUIRE(s, USTB_E_ARG, "NULL server");
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        s->stop = true;
+    }
+    s->cv_queue.notify_all();
+    s->scheduler.join();
+    s->completer.join();
+    int rc = USTB_OK;
+    if (s->stream) {
+        const cudaError_t e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) rc = ustb::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+        cudaStreamDestroy(s->stream);
+    }
+    if (s->workspace) cudaFree(s->workspace);
+    if (s->scratch) cudaFree(s->scratch);
+    if (s->host_flags) cudaFreeHost(s->host_flags);
+    delete s;
+    return rc;
+}
