@@ -347,15 +347,16 @@ int ustb_plan_execute(ustb_plan plan, const void* ch, const ustb_das_outputs* ou
  * done) and returns at once with a ticket.  A scheduler thread takes queued
  * requests in arrival order into batches whose interpolation entries fit
  * `workspace_budget` bytes (at most `max_batch` requests, at most 40) and launches
- * each batch as ustb_das_fast_batch_ws on the server's own stream, from a
- * workspace the server owns; a completion thread waits for each batch and marks
- * its tickets done.  A request whose entries alone exceed the budget runs in a
- * batch of its own.  The reference serves no requests: das.m beamforms one call
+ * each batch as ustb_das_fast_batch_ws, alternating between two streams of its
+ * own with a workspace each; a completion thread waits for each batch and marks
+ * its tickets done.  A request whose entries alone exceed the budget, or with more
+ * than `large_units` pixel x channel x wave x frame units (0: 2e9), runs in a
+ * batch of its own, so small requests never wait for a large one's launch.  The reference serves no requests: das.m beamforms one call
  * at a time.
  */
 typedef struct ustb_server_s* ustb_server;
 
-int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, ustb_server* server);
+int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, int64_t large_units, ustb_server* server);
 int ustb_serve_submit(ustb_server server, ustb_plan plan, const void* ch, const ustb_das_outputs* out,
                       uint64_t* ticket);
 /* Wait until the ticket's request is done (timeout_ms < 0: no limit); USTB_E_TIMEOUT

@@ -3,11 +3,13 @@
 // Requests are queued by ustb_serve_submit (any thread).  A scheduler thread takes
 // them in arrival order into batches whose interpolation entries fit the workspace
 // budget (at most max_batch requests), launches each batch with
-// ustb_das_fast_batch_ws on the server's stream from the server's workspace, copies
-// the batch's flag word to pinned host memory and records an event.  A completion
-// thread waits for the events in launch order and marks the batches' tickets done.
-// Batches run back to back on one stream, so one workspace serves every batch: a
-// batch's entries pass only starts once the previous batch's kernels are done.
+// ustb_das_fast_batch_ws, copies the batch's flag word to pinned host memory and
+// records an event.  A completion thread waits for the events in launch order and
+// marks the batches' tickets done.  Batches alternate between two streams, each
+// with its own workspace and queue counters, so one batch's entries pass overlaps
+// the tail of the previous batch's beamforming; on one stream, a batch's entries
+// pass only starts once the previous batch there is done, so each workspace is
+// reused safely.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +34,7 @@ namespace {
 
 constexpr int kMaxBatchRequests = 40;  // the persistent kernel's request table
 constexpr int kFlagSlots = 64;         // pinned flag words (batches in flight at most)
+constexpr int kStreams = 2;            // batches alternate between these
 
 struct Job {
     uint64_t ticket;
@@ -67,12 +70,14 @@ struct ustb_server_s {
     bool stop = false;           // destroy requested: finish the queue, then exit
     bool sched_exited = false;   // the scheduler has launched everything it will
     int64_t budget = 0;
+    int64_t large_units = 0;  // requests above this many units launch alone
     int max_batch = 1;
     int device = 0;
-    cudaStream_t stream = nullptr;
-    void* workspace = nullptr;
-    int64_t ws_bytes = 0;
-    uint64_t* scratch = nullptr;  // device: flag word + queue counters
+    cudaStream_t stream[kStreams] = {};
+    void* workspace[kStreams] = {};
+    int64_t ws_bytes[kStreams] = {};
+    uint64_t* scratch[kStreams] = {};  // device: flag word + queue counters
+    int next = 0;                      // stream of the next batch
     uint64_t* host_flags = nullptr;  // pinned [kFlagSlots]
     std::vector<int> free_slots;
     std::thread scheduler, completer;
@@ -87,19 +92,22 @@ int ustb_server_s::launch(const std::vector<Job>& jobs, Batch& b) {
     for (size_t i = 0; i < jobs.size(); ++i) ustb::plan_request(jobs[i].plan, jobs[i].ch, &jobs[i].out, &reqs[i]);
     const int64_t need = ustb_das_fast_workspace_bytes(reqs.data(), (int32_t)reqs.size());
     if (need < 0) return (int)-need;
-    if (need > ws_bytes) {  // grow: the stream must be idle before the old block goes
-        USTB_CUDA(cudaStreamSynchronize(stream));
-        if (workspace) USTB_CUDA(cudaFree(workspace));
-        workspace = nullptr;
-        ws_bytes = 0;
-        USTB_CUDA(cudaMalloc(&workspace, (size_t)need));
-        ws_bytes = need;
+    const int i = next;
+    next = (next + 1) % kStreams;
+    if (need > ws_bytes[i]) {  // grow: the stream must be idle before the old block goes
+        USTB_CUDA(cudaStreamSynchronize(stream[i]));
+        if (workspace[i]) USTB_CUDA(cudaFree(workspace[i]));
+        workspace[i] = nullptr;
+        ws_bytes[i] = 0;
+        USTB_CUDA(cudaMalloc(&workspace[i], (size_t)need));
+        ws_bytes[i] = need;
     }
-    const int rc = ustb_das_fast_batch_ws(reqs.data(), (int32_t)reqs.size(), scratch, workspace, ws_bytes, stream);
+    const int rc = ustb_das_fast_batch_ws(reqs.data(), (int32_t)reqs.size(), scratch[i], workspace[i], ws_bytes[i],
+                                          stream[i]);
     if (rc != USTB_OK) return rc;
-    USTB_CUDA(cudaMemcpyAsync(host_flags + b.slot, scratch, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+    USTB_CUDA(cudaMemcpyAsync(host_flags + b.slot, scratch[i], sizeof(uint64_t), cudaMemcpyDeviceToHost, stream[i]));
     USTB_CUDA(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming | cudaEventBlockingSync));
-    USTB_CUDA(cudaEventRecord(b.ev, stream));
+    USTB_CUDA(cudaEventRecord(b.ev, stream[i]));
     return USTB_OK;
 }
 
@@ -115,16 +123,19 @@ void ustb_server_s::schedule() {
             cv_flight.wait(lk, [&] { return !free_slots.empty(); });
             slot = free_slots.back();
             free_slots.pop_back();
-            // arrival order; add requests while their entries fit the budget
+            // arrival order; add requests while their entries fit the budget.  A large
+            // request launches alone, so small ones never share (and wait for) its tail.
             int64_t bytes = 0;
             while (!queue.empty() && (int)jobs.size() < max_batch) {
                 ustb_das_request r;
                 ustb::plan_request(queue.front().plan, queue.front().ch, &queue.front().out, &r);
                 const int64_t b = ustb_das_fast_workspace_bytes(&r, 1);
-                if (!jobs.empty() && bytes + b > budget) break;
+                const bool large = r.L > 0 && (double)r.geometry->n_pixels * r.N * r.W * r.F > (double)large_units;
+                if (!jobs.empty() && (large || bytes + b > budget)) break;
                 bytes += b;
                 jobs.push_back(queue.front());
                 queue.pop_front();
+                if (large) break;
             }
         }
         Batch b;
@@ -177,7 +188,8 @@ void ustb_server_s::complete() {
     }
 }
 
-extern "C" int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, ustb_server* out) {
+extern "C" int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, int64_t large_units,
+                                 ustb_server* out) {
     ustb::clear_error();
     USTB_REQUIRE(out, USTB_E_ARG, "NULL pointer");
     *out = nullptr;
@@ -187,9 +199,12 @@ extern "C" int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, us
     std::unique_ptr<ustb_server_s> s(new ustb_server_s());
     s->budget = workspace_budget;
     s->max_batch = max_batch;
+    s->large_units = large_units > 0 ? large_units : (int64_t)2000000000;
     USTB_CUDA(cudaGetDevice(&s->device));
-    USTB_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-    USTB_CUDA(cudaMalloc(&s->scratch, sizeof(uint64_t) * (kMaxBatchRequests + 1)));
+    for (int i = 0; i < kStreams; ++i) {
+        USTB_CUDA(cudaStreamCreateWithFlags(&s->stream[i], cudaStreamNonBlocking));
+        USTB_CUDA(cudaMalloc(&s->scratch[i], sizeof(uint64_t) * (kMaxBatchRequests + 1)));
+    }
     USTB_CUDA(cudaHostAlloc(&s->host_flags, sizeof(uint64_t) * kFlagSlots, cudaHostAllocDefault));
     for (int i = kFlagSlots - 1; i >= 0; --i) s->free_slots.push_back(i);
     ustb_server_s* raw = s.get();
@@ -252,13 +267,15 @@ extern "C" int ustb_serve_destroy(ustb_server s) {
     s->scheduler.join();
     s->completer.join();
     int rc = USTB_OK;
-    if (s->stream) {
-        const cudaError_t e = cudaStreamSynchronize(s->stream);
-        if (e != cudaSuccess) rc = ustb::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
-        cudaStreamDestroy(s->stream);
+    for (int i = 0; i < kStreams; ++i) {
+        if (s->stream[i]) {
+            const cudaError_t e = cudaStreamSynchronize(s->stream[i]);
+            if (e != cudaSuccess && rc == USTB_OK) rc = ustb::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+            cudaStreamDestroy(s->stream[i]);
+        }
+        if (s->workspace[i]) cudaFree(s->workspace[i]);
+        if (s->scratch[i]) cudaFree(s->scratch[i]);
     }
-    if (s->workspace) cudaFree(s->workspace);
-    if (s->scratch) cudaFree(s->scratch);
     if (s->host_flags) cudaFreeHost(s->host_flags);
     delete s;
     return rc;
