@@ -85,6 +85,15 @@ struct ustb_server_s {
     void schedule();
     void complete();
     int launch(const std::vector<Job>& jobs, Batch& b);
+    // CUDA resources (also after a failed create); the threads are joined first
+    ~ustb_server_s() {
+        for (int i = 0; i < kStreams; ++i) {
+            if (stream[i]) cudaStreamDestroy(stream[i]);
+            if (workspace[i]) cudaFree(workspace[i]);
+            if (scratch[i]) cudaFree(scratch[i]);
+        }
+        if (host_flags) cudaFreeHost(host_flags);
+    }
 };
 
 int ustb_server_s::launch(const std::vector<Job>& jobs, Batch& b) {
@@ -268,15 +277,10 @@ extern "C" int ustb_serve_destroy(ustb_server s) {
     s->completer.join();
     int rc = USTB_OK;
     for (int i = 0; i < kStreams; ++i) {
-        if (s->stream[i]) {
-            const cudaError_t e = cudaStreamSynchronize(s->stream[i]);
-            if (e != cudaSuccess && rc == USTB_OK) rc = ustb::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
-            cudaStreamDestroy(s->stream[i]);
-        }
-        if (s->workspace[i]) cudaFree(s->workspace[i]);
-        if (s->scratch[i]) cudaFree(s->scratch[i]);
+        if (!s->stream[i]) continue;
+        const cudaError_t e = cudaStreamSynchronize(s->stream[i]);
+        if (e != cudaSuccess && rc == USTB_OK) rc = ustb::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
     }
-    if (s->host_flags) cudaFreeHost(s->host_flags);
-    delete s;
+    delete s;  // frees the streams, workspaces and pinned flags
     return rc;
 }
