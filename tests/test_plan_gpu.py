@@ -151,3 +151,60 @@ def test_destroy_finishes_queued_requests(workloads):
     torch.cuda.synchronize()
     for o, _ in outs:
         assert rel(o["cube"], w["ref"]["cube"]) <= TOL
+
+
+# ---- plans on geometry the library tiles by other rules --------------------------
+
+def _case(cuda_dev, seq, scan, rx, seed):
+    from ustb_gb300.uff import Probe
+
+    rng = np.random.default_rng(seed)
+    N, L = 16, 640
+    probe = Probe.linear_array(N, 0.3e-3)
+    fs, f0, c = 20e6, 5e6, 1540.0
+    x = (rng.standard_normal((L, N, len(seq))) + 1j * rng.standard_normal((L, N, len(seq)))).astype(np.complex64)
+    k = np.array([1, 4, 6, 4, 1], np.float32) / 16
+    x = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 0, x).astype(np.complex64)
+    ph = np.exp(-1j * 4 * np.pi * f0 * scan.reference_distance / c)
+    g = fast.FastGeometry(probe, scan, seq, fs, 0.0, f0, c, cuda_dev, rx, None, pixel_phase=ph)
+    t = torch.from_numpy(np.ascontiguousarray(x[..., None].transpose(3, 2, 1, 0))).to(cuda_dev)
+    st = fast.convert_channels(t, Precision.fp32)
+    ref = fast.das_fast(st, Precision.fp32, True, g, 3, L=L)["cube"]
+    p = Plan(g, L, Precision.fp32, True, 3)
+    got = p.execute(st)
+    torch.cuda.synchronize()
+    return g, p, got, ref
+
+
+def test_plan_with_table_waves_and_receive_table(cuda_dev):
+    """Focused waves whose focal band crosses the scan take their delays from the
+    table (the library re-splits tiles by the tabulated span), and a receive window
+    without a closed form (sta) comes from the receive table."""
+    from ustb_gb300.enums import Window
+    from ustb_gb300.uff import LinearScan, Point, Wave
+
+    scan = LinearScan(np.linspace(-3e-3, 3e-3, 24), np.linspace(5e-3, 14e-3, 40))
+    seq = [Wave(source=Point.from_xyz(x, 0, 9e-3)) for x in (-1e-3, 0.0, 1e-3)]
+    rx = Apodization(window=Window.sta, origin=Point.from_xyz(0.0, 0, 0))
+    g, p, got, ref = _case(cuda_dev, seq, scan, rx, 21)
+    assert g.d_txdelay is not None and g.d_rxapo is not None
+    assert int(got["flags"].item()) == 0
+    assert rel(got["cube"], ref) <= TOL
+    p.close()
+
+
+def test_plan_on_a_pixel_list(cuda_dev):
+    """Pixels given as a list (no grid): the library orders them on a coarse spatial
+    grid and cuts runs of 512."""
+    from ustb_gb300.enums import Window
+    from ustb_gb300.uff import Scan, Wave
+
+    rng = np.random.default_rng(22)
+    P = 3000
+    scan = Scan(rng.uniform(-3e-3, 3e-3, P), np.zeros(P), rng.uniform(5e-3, 14e-3, P))
+    seq = [Wave.plane(a) for a in np.deg2rad([-8.0, 0.0, 8.0])]
+    g, p, got, ref = _case(cuda_dev, seq, scan, Apodization(window=Window.tukey25, f_number=1.5), 22)
+    assert int(got["flags"].item()) == 0
+    assert p.n_tiles >= 6  # 3000 pixels in tiles of at most 512
+    assert rel(got["cube"], ref) <= TOL
+    p.close()
