@@ -720,6 +720,37 @@ def profile_post(args, torch):
     print(json.dumps(out), flush=True)
 
 
+def profile_small(args, torch):
+    """--profile small: the HBM-bound helper kernels at sizes above L2.
+    convert:  the headline channel data, complex64 -> FP16 (78.6 MB in, 39.3 MB out);
+    phase:    the per-pixel phase on 200 frames of a 131,072-pixel complex image (210 MB);
+    fir:      the sDMAS band-pass along depth of 200 frames x 256 columns x 512 depths
+              (105 MB), Kaiser band-pass 3-5 MHz (0.5 MHz transitions) at 48 MHz."""
+    from ustb_gb300 import fast, kernels, postprocess
+    from ustb_gb300.enums import Precision
+
+    dev = torch.device("cuda", 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    _, _, ch = make_headline(dev)
+    g = torch.Generator(device=dev).manual_seed(3)
+    img = torch.randn((200, 131072), dtype=torch.complex64, device=dev, generator=g)  # (F, P)
+    ph = torch.exp(1j * torch.rand(131072, device=dev, generator=g) * 6.28).to(torch.complex64)
+    col = torch.randn((200 * 256, 512), device=dev, generator=g)
+    taps = postprocess.bandpass_taps([2.5e6, 3e6, 5e6, 5.5e6], 48e6)
+    steps = {"convert": lambda: fast.convert_channels(ch, Precision.fp16),
+             "phase": lambda: kernels.apply_pixel_phase(img, ph),
+             "fir": lambda: postprocess.fir_depth(col, taps)}
+    out = {"profile": "small", "bytes": {"convert": int(ch.numel() * 8 + ch.numel() * 4),
+                                         "phase": int(img.numel() * 16 + ph.numel() * 8),
+                                         "fir": int(col.numel() * 8)}, "fir_taps": int(len(taps))}
+    for name, fn in steps.items():
+        for _ in range(args.warmup):
+            fn()
+        out[name + "_ms"] = [round(t, 4) for t in cuda_time(fn, args.steps, flush, stream, torch)]
+    print(json.dumps(out), flush=True)
+
+
 def profile_ensemble(args, torch):
     """--profile ensemble: the persistent batch kernel on a 20-frame slice of the
     high-frame-rate ensemble (20 frames x 11 plane waves x 128 channels x 1536 int16 I/Q
@@ -756,6 +787,8 @@ def main_profile(args):
         return profile_post(args, torch)
     if args.profile == "ensemble":
         return profile_ensemble(args, torch)
+    if args.profile == "small":
+        return profile_small(args, torch)
 
     from ustb_gb300 import fast, geometry, kernels, synth
     from ustb_gb300.enums import Precision
