@@ -10,9 +10,12 @@
 //
 // One CTA computes kout (<= 1024) consecutive outputs of one trace: it stages the
 // taps and the mixed samples the outputs need (kout*D + ntaps - 1 of them, at most
-// about 8192) in shared memory, the samples in polyphase order (phase-major) so that the
-// 32 outputs of a warp read 32 consecutive samples for each tap; each thread forms 4
-// outputs with independent accumulators.  The mixer phase
+// about 8192) in shared memory, the samples in polyphase order (phase-major): output o
+// reads, for tap k, position o + (last - k)/D of row (last - k) % D, so the taps of one
+// row step one position at a time.  Each thread forms 4 consecutive outputs and, per
+// block of 4 taps of a row, loads the 7 samples they span once (a shared load per
+// 4.6 FMA instead of per 2); a float2 of padding after every 16 keeps the half-warps'
+// loads on distinct banks.  The mixer phase
 // is formed in cycles as c0 + j*step with step split into two floats and the
 // product's rounding error recovered by an FMA, so the phase stays exact to
 // ~1e-7 cycles over any trace length.
@@ -35,7 +38,12 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kOPT = 4;                  // outputs per thread
+constexpr int kOPT = 4;                  // consecutive outputs per thread
+constexpr int kTB = 4;                   // taps per register block
+
+// staged row position q with one float2 of padding after every 16, so that the 16
+// lanes of a half-warp, whose first outputs are 4 apart, read 16 different bank pairs
+__device__ __forceinline__ int row_pad(int q) { return q + (q >> 4); }
 constexpr int kStage = 8192;             // staged samples per CTA at most (64 KB), when kout allows
 
 template <typename S>
@@ -87,6 +95,7 @@ struct DemodArgs {
     int64_t L, Ld, n_traces;
     int D, ntaps, kout;  // kout: outputs per CTA (<= kThreads * kOPT)
     int mb, shift;         // zero-phase: taps of the reference filter, and mb - 1
+    int Qa, Qp;            // staged samples per polyphase row, and the padded row stride
     float c0;              // fractional part of fc * t0 (cycles)
     float step_hi, step_lo;  // fc / fs split into two floats
     float scale;
@@ -164,9 +173,11 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     const int off = (int)((((trace * a.L + j0 + a.shift) % 4) + 4) % 4);
     const int64_t jb = j0 - off;
     const int nstage = a.kout * a.D + a.ntaps - 1 + off;
-    // the staged samples are stored polyphase: sample s at mix[(s % D) * Q + s / D], so
-    // that for one tap the 32 outputs of a warp read 32 consecutive float2
-    const int Q = (nstage + a.D - 1) / a.D;
+    // the staged samples are stored polyphase: sample s at mix[(s % D) * Qp + row_pad(s / D)];
+    // the rows' tails, read by the last outputs' padded tap blocks, are zeros
+    const int Qp = a.Qp;
+    for (int t = nstage + threadIdx.x; t < a.Qa * a.D; t += kThreads)
+        mix[(t % a.D) * Qp + row_pad(t / a.D)] = make_float2(0.f, 0.f);
     for (int s0 = 4 * threadIdx.x; s0 < nstage; s0 += 4 * kThreads) {
         const int64_t jv = jb + s0 + a.shift;  // trace index of staged sample s0
         float2 v[4];
@@ -184,47 +195,54 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
         for (int u = 0; u < 4; ++u) {
             const int s = s0 + u;
             if (s >= nstage) break;
-            mix[(s % a.D) * Q + s / a.D] = v[u];  // polyphase: phase-major
+            mix[(s % a.D) * Qp + row_pad(s / a.D)] = v[u];  // polyphase: phase-major
         }
     }
     __syncthreads();
-    // outputs o = threadIdx.x + kThreads * q, kOPT per thread: independent accumulators
+    // kOPT consecutive outputs per thread.  Output o at tap k reads staged sample
+    // o*D + last - k, i.e. row (last - k) % D at o + (last - k) / D: the taps of one
+    // row, k = last - ph - m*D, step the read position by one.  For each block of kTB
+    // taps of a row the thread loads the kOPT + kTB - 1 samples they span once.
     float2 acc[kOPT];
 #pragma unroll
     for (int q = 0; q < kOPT; ++q) acc[q] = make_float2(0.f, 0.f);
     const int last = a.ntaps - 1 + off;
-    // tap k reads staged sample o*D + last - k: phase (last - k) % D, offset (last - k) / D,
-    // stepped down incrementally instead of divided per tap
-    auto fir = [&](auto full) {
-        int ph = last % a.D, qo = last / a.D;
-        for (int k = 0; k < a.ntaps; ++k) {
-            const float b = tap[k];
-            const float2* row = mix + ph * Q + qo;
+    const int o0 = threadIdx.x * kOPT;
+    if (o0 < a.kout) {
+        for (int ph = 0; ph < a.D && ph <= last; ++ph) {
+            const int mhi = (last - ph) / a.D;                                   // tap k = last - ph - m D >= 0
+            const int mlo = max(0, (last - ph - (a.ntaps - 1) + a.D - 1) / a.D);  // and <= ntaps - 1
+            const float2* row = mix + ph * Qp;
+            for (int m0 = mlo; m0 <= mhi; m0 += kTB) {
+                float2 v[kOPT + kTB - 1];
 #pragma unroll
-            for (int q = 0; q < kOPT; ++q) {
-                const int o = threadIdx.x + kThreads * q;
-                if (decltype(full)::value || o < a.kout) {
-                    const float2 v = row[o];
-                    acc[q].x = fmaf(b, v.x, acc[q].x);
-                    acc[q].y = fmaf(b, v.y, acc[q].y);
+                for (int j = 0; j < kOPT + kTB - 1; ++j) v[j] = row[row_pad(o0 + m0 + j)];
+#pragma unroll
+                for (int mm = 0; mm < kTB; ++mm) {
+                    const int m = m0 + mm;
+                    const float b = m <= mhi ? tap[last - ph - m * a.D] : 0.f;
+#pragma unroll
+                    for (int q = 0; q < kOPT; ++q) {
+                        acc[q].x = fmaf(b, v[q + mm].x, acc[q].x);
+                        acc[q].y = fmaf(b, v[q + mm].y, acc[q].y);
+                    }
                 }
             }
-            if (ph == 0) {
-                ph = a.D - 1;
-                --qo;
-            } else {
-                --ph;
-            }
         }
-    };
-    if (a.kout == kThreads * kOPT) fir(std::true_type{});
-    else fir(std::false_type{});
+    }
 #pragma unroll
     for (int q = 0; q < kOPT; ++q) {
-        const int o = threadIdx.x + kThreads * q;
+        const int o = o0 + q;
         const int64_t m = m0 + o;
         if (o < a.kout && m < a.Ld) store_iq<D>(iq, trace * a.Ld + m, acc[q]);
     }
+}
+
+// staged row length and padded stride: the rows hold the chunk's samples and the
+// farthest position a thread's last tap block reads, o + m + j < kout + (ntaps + 2)/D + kOPT + kTB
+void set_rows(DemodArgs& a) {
+    a.Qa = a.kout + (a.ntaps + 2) / a.D + kOPT + kTB;
+    a.Qp = (a.Qa - 1) + ((a.Qa - 1) >> 4) + 1;
 }
 
 // outputs per CTA: the trace's Ld outputs split into the fewest chunks of at most kmax,
@@ -239,7 +257,7 @@ int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, con
     const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t blocks = chunks * a.n_traces;
     USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
-    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + (size_t)(a.kout * a.D + a.ntaps - 1 + 3) + a.D);
+    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + (size_t)a.D * (size_t)a.Qp);
     int dev = 0, optin = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -286,6 +304,7 @@ extern "C" int ustb_demodulate(const void* rf, int32_t src_type, void* iq, int32
     a.D = decimation;
     a.ntaps = ntaps;
     a.kout = balanced_chunk(a.Ld, std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - ntaps) / decimation)));
+    set_rows(a);
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;
@@ -334,6 +353,7 @@ extern "C" int ustb_demodulate_filtfilt(const void* rf, int32_t src_type, void* 
     a.mb = ntaps;
     a.shift = ntaps - 1;
     a.kout = balanced_chunk(a.Ld, std::max<int64_t>(32, std::min<int64_t>(kThreads * kOPT, (kStage - a.ntaps) / decimation)));
+    set_rows(a);
     const double c0 = fc * t0;
     a.c0 = (float)(c0 - std::floor(c0));
     const double step = fc / fs;
