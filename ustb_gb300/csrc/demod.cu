@@ -39,7 +39,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kOPT = 4;                  // consecutive outputs per thread
-constexpr int kTB = 4;                   // taps per register block
+constexpr int kTB = 4;                   // taps per register block (one float4 of a tap row)
+static_assert(kTB == 4, "a tap block is read as one float4");
 
 // staged row position q with one float2 of padding after every 16, so that the 16
 // lanes of a half-warp, whose first outputs are 4 apart, read 16 different bank pairs
@@ -96,6 +97,7 @@ struct DemodArgs {
     int D, ntaps, kout;  // kout: outputs per CTA (<= kThreads * kOPT)
     int mb, shift;         // zero-phase: taps of the reference filter, and mb - 1
     int Qa, Qp;            // staged samples per polyphase row, and the padded row stride
+    int T4, Cap;           // taps rounded up to 4; taps per polyphase row (a multiple of 4)
     float c0;              // fractional part of fc * t0 (cycles)
     float step_hi, step_lo;  // fc / fs split into two floats
     float scale;
@@ -137,8 +139,9 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
                                                          const float* __restrict__ taps, const DemodArgs a) {
     // shared: taps[ntaps], then the mixed samples [kout * D + ntaps - 1]
     extern __shared__ float2 smem2[];
-    float* tap = reinterpret_cast<float*>(smem2);
-    float2* mix = smem2 + (a.ntaps + 1) / 2;
+    float* tap = reinterpret_cast<float*>(smem2);  // zero-phase: the taps formed per CTA
+    float* trow = tap + a.T4;                       // taps by polyphase row, zero-padded
+    float2* mix = reinterpret_cast<float2*>(trow + a.D * a.Cap);
     const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t trace = blockIdx.x / chunks;
     const int64_t m0 = (blockIdx.x - trace * chunks) * a.kout;
@@ -162,8 +165,6 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
             if (k < a.ntaps && !(i & 1)) tap[k] = h;
         }
         __syncthreads();
-    } else {
-        for (int k = threadIdx.x; k < a.ntaps; k += kThreads) tap[k] = __ldg(taps + k);
     }
     const S* x = rf + trace * a.L;
     // staged window [j0, j0 + nstage) of the filtered sequence, whose sample j is
@@ -176,6 +177,15 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     // the staged samples are stored polyphase: sample s at mix[(s % D) * Qp + row_pad(s / D)];
     // the rows' tails, read by the last outputs' padded tap blocks, are zeros
     const int Qp = a.Qp;
+    // tap k belongs to row (last - k) % D at m = (last - k) / D: trow[ph][m]
+    const int last = a.ntaps - 1 + off;
+    for (int i = threadIdx.x; i < a.D * a.Cap; i += kThreads) {
+        const int ph = i / a.Cap, m = i - ph * a.Cap;
+        const int k = last - ph - m * a.D;
+        float b = 0.f;
+        if (k >= 0 && k < a.ntaps) b = ZP ? tap[k] : __ldg(taps + k);
+        trow[i] = b;
+    }
     for (int t = nstage + threadIdx.x; t < a.Qa * a.D; t += kThreads)
         mix[(t % a.D) * Qp + row_pad(t / a.D)] = make_float2(0.f, 0.f);
     for (int s0 = 4 * threadIdx.x; s0 < nstage; s0 += 4 * kThreads) {
@@ -206,25 +216,24 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
     float2 acc[kOPT];
 #pragma unroll
     for (int q = 0; q < kOPT; ++q) acc[q] = make_float2(0.f, 0.f);
-    const int last = a.ntaps - 1 + off;
     const int o0 = threadIdx.x * kOPT;
     if (o0 < a.kout) {
         for (int ph = 0; ph < a.D && ph <= last; ++ph) {
-            const int mhi = (last - ph) / a.D;                                   // tap k = last - ph - m D >= 0
-            const int mlo = max(0, (last - ph - (a.ntaps - 1) + a.D - 1) / a.D);  // and <= ntaps - 1
+            const int mhi = (last - ph) / a.D;  // taps k = last - ph - m D >= 0 (zero where k >= ntaps)
             const float2* row = mix + ph * Qp;
-            for (int m0 = mlo; m0 <= mhi; m0 += kTB) {
+            const float* tr = trow + ph * a.Cap;
+            for (int m0 = 0; m0 <= mhi; m0 += kTB) {
+                const float4 b4 = *reinterpret_cast<const float4*>(tr + m0);
+                const float bb[kTB] = {b4.x, b4.y, b4.z, b4.w};
                 float2 v[kOPT + kTB - 1];
 #pragma unroll
                 for (int j = 0; j < kOPT + kTB - 1; ++j) v[j] = row[row_pad(o0 + m0 + j)];
 #pragma unroll
                 for (int mm = 0; mm < kTB; ++mm) {
-                    const int m = m0 + mm;
-                    const float b = m <= mhi ? tap[last - ph - m * a.D] : 0.f;
 #pragma unroll
                     for (int q = 0; q < kOPT; ++q) {
-                        acc[q].x = fmaf(b, v[q + mm].x, acc[q].x);
-                        acc[q].y = fmaf(b, v[q + mm].y, acc[q].y);
+                        acc[q].x = fmaf(bb[mm], v[q + mm].x, acc[q].x);
+                        acc[q].y = fmaf(bb[mm], v[q + mm].y, acc[q].y);
                     }
                 }
             }
@@ -243,6 +252,8 @@ __global__ void __launch_bounds__(kThreads) demod_kernel(const S* __restrict__ r
 void set_rows(DemodArgs& a) {
     a.Qa = a.kout + (a.ntaps + 2) / a.D + kOPT + kTB;
     a.Qp = (a.Qa - 1) + ((a.Qa - 1) >> 4) + 1;
+    a.T4 = (a.ntaps + 3) / 4 * 4;
+    a.Cap = ((a.ntaps + 2) / a.D + 1 + 3) / 4 * 4;  // m <= (ntaps - 1 + 3) / D
 }
 
 // outputs per CTA: the trace's Ld outputs split into the fewest chunks of at most kmax,
@@ -257,7 +268,8 @@ int launch_demod(const S* rf, void* iq, int32_t dst_type, const float* taps, con
     const int64_t chunks = (a.Ld + a.kout - 1) / a.kout;
     const int64_t blocks = chunks * a.n_traces;
     USTB_REQUIRE(blocks <= INT32_MAX, USTB_E_SHAPE, "too many traces x output chunks");
-    const size_t smem = sizeof(float2) * ((size_t)(a.ntaps + 1) / 2 + (size_t)a.D * (size_t)a.Qp);
+    const size_t smem = sizeof(float) * ((size_t)a.T4 + (size_t)a.D * (size_t)a.Cap) +
+                        sizeof(float2) * (size_t)a.D * (size_t)a.Qp;
     int dev = 0, optin = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
