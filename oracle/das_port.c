@@ -19,7 +19,7 @@
  *                    two agree bit for bit (pinned in tests/test_oracle.py).
  *
  *  oracle_das_f64  — the same formula in double precision (the "FP64 oracle"
- *                    the reduced-precision GPU path is judged against).  Takes
+ *                    the reduced-precision GPU path is checked against).  Takes
  *                    double tables and data.  edge_rule 0 = das_c's validity
  *                    rule; 1 = the tools.matlab_beamformer / interp1 rule
  *                    (+tools/matlab_beamformer.m:30: t in [t_0, t_{L-1}]).
