@@ -333,6 +333,10 @@ typedef struct {
 
 /* Copy the geometry to the device and plan its tiles.  Synchronous. */
 int ustb_plan_create(const ustb_plan_desc* desc, ustb_plan* plan);
+/* The tile map ustb_plan_create would use for this descriptor, planned on the host
+ * without a GPU: up to `capacity` tiles of USTB_TILE_PIXELS lanes are written to the
+ * host array `tiles` (may be NULL); returns the number of tiles, or -status. */
+int64_t ustb_plan_tiles_host(const ustb_plan_desc* desc, int32_t* tiles, int64_t capacity);
 /* Free a plan's device memory.  No call that uses the plan may still be in flight. */
 int ustb_plan_destroy(ustb_plan plan);
 /* Number of tiles of a plan (negative status on a NULL plan). */

@@ -291,10 +291,9 @@ struct ustb_plan_s {
     }
 };
 
-extern "C" int ustb_plan_create(const ustb_plan_desc* d, ustb_plan* out) {
-    ustb::clear_error();
-    USTB_REQUIRE(d && out, USTB_E_ARG, "NULL pointer");
-    *out = nullptr;
+// checks a descriptor and builds (or checks) its tile map; host only
+static int plan_tiles(const ustb_plan_desc* d, std::vector<int32_t>& tiles, int64_t& T) {
+    USTB_REQUIRE(d, USTB_E_ARG, "NULL pointer");
     const ustb_das_geometry& h = d->geometry;
     USTB_REQUIRE(h.element_xyz && h.pixel_xyz && h.waves, USTB_E_ARG, "geometry needs element, pixel and wave arrays");
     USTB_REQUIRE(h.n_elements >= 1 && h.n_pixels >= 1 && h.n_waves >= 1, USTB_E_SHAPE, "empty geometry");
@@ -313,14 +312,12 @@ extern "C" int ustb_plan_create(const ustb_plan_desc* d, ustb_plan* out) {
         tables |= h.waves[w].kind == USTB_WAVE_TABLE;
     }
     USTB_REQUIRE(!tables || h.tx_delay_table, USTB_E_ARG, "table waves need tx_delay_table");
-    const int64_t P = h.n_pixels, N = h.n_elements, W = h.n_waves;
+    const int64_t P = h.n_pixels;
     const int64_t* gr = d->pixel_grid;
     USTB_REQUIRE((gr[0] == 0 && gr[1] == 0 && gr[2] == 0) || (gr[0] > 0 && gr[1] > 0 && gr[2] > 0 && gr[0] * gr[1] * gr[2] == P),
                  USTB_E_SHAPE, "pixel_grid must multiply to n_pixels (or be all zero)");
-
-    // tile map
-    std::vector<int32_t> tiles;
-    int64_t T = 0;
+    tiles.clear();
+    T = 0;
     if (h.tile_pixels) {
         T = h.n_tiles;
         USTB_REQUIRE(T >= 1, USTB_E_SHAPE, "tile_pixels given with n_tiles < 1");
@@ -332,16 +329,39 @@ extern "C" int ustb_plan_create(const ustb_plan_desc* d, ustb_plan* out) {
                 USTB_REQUIRE(tiles[t * kTile + j] >= -1 && tiles[t * kTile + j] < P, USTB_E_ARG,
                              "tile %lld lane %d: pixel index out of range", (long long)t, j);
         }
-    } else {
-        const Pts p{h.pixel_xyz};
-        const double limit = kSpanLimit * (double)h.sound_speed / (double)h.fs;
-        std::vector<std::vector<int32_t>> blocks = plan_blocks(p, P, gr, limit);
-        refine_by_table(blocks, h, P);
-        order_by_cost(blocks, h);
-        T = (int64_t)blocks.size();
-        tiles.assign((size_t)(T * kTile), -1);
-        for (int64_t t = 0; t < T; ++t) std::copy(blocks[t].begin(), blocks[t].end(), tiles.begin() + t * kTile);
+        return USTB_OK;
     }
+    const Pts p{h.pixel_xyz};
+    const double limit = kSpanLimit * (double)h.sound_speed / (double)h.fs;
+    std::vector<std::vector<int32_t>> blocks = plan_blocks(p, P, gr, limit);
+    refine_by_table(blocks, h, P);
+    order_by_cost(blocks, h);
+    T = (int64_t)blocks.size();
+    tiles.assign((size_t)(T * kTile), -1);
+    for (int64_t t = 0; t < T; ++t) std::copy(blocks[t].begin(), blocks[t].end(), tiles.begin() + t * kTile);
+    return USTB_OK;
+}
+
+extern "C" int64_t ustb_plan_tiles_host(const ustb_plan_desc* d, int32_t* out, int64_t capacity) {
+    ustb::clear_error();
+    std::vector<int32_t> tiles;
+    int64_t T = 0;
+    const int rc = plan_tiles(d, tiles, T);
+    if (rc != USTB_OK) return -rc;
+    if (out) std::copy(tiles.begin(), tiles.begin() + std::min(T, std::max<int64_t>(capacity, 0)) * kTile, out);
+    return T;
+}
+
+extern "C" int ustb_plan_create(const ustb_plan_desc* d, ustb_plan* out) {
+    ustb::clear_error();
+    USTB_REQUIRE(d && out, USTB_E_ARG, "NULL pointer");
+    *out = nullptr;
+    std::vector<int32_t> tiles;
+    int64_t T = 0;
+    const int prc = plan_tiles(d, tiles, T);
+    if (prc != USTB_OK) return prc;
+    const ustb_das_geometry& h = d->geometry;
+    const int64_t P = h.n_pixels, N = h.n_elements, W = h.n_waves;
 
     std::unique_ptr<ustb_plan_s> pl(new ustb_plan_s());
     USTB_CUDA(cudaGetDevice(&pl->device));

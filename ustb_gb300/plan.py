@@ -45,6 +45,47 @@ def _host(t: Optional[torch.Tensor], keep: list) -> Optional[int]:
     return h.data_ptr()
 
 
+def plan_desc(geom: FastGeometry, L: int, precision: Precision, is_complex: bool, dimension=Dimension.both,
+              F: int = 1, epilogue: bool = False, library_tiles: bool = True):
+    """(CPlanDesc with host pointers, the host arrays it points into) for a geometry."""
+    keep = []
+    d = CPlanDesc()
+    g = CGeometry()
+    ctypes.pointer(g)[0] = geom.c  # copy the scalar fields
+    g.element_xyz = _host(geom.d_el, keep)
+    g.pixel_xyz = _host(geom.d_px, keep)
+    g.waves = _host(geom.d_waves, keep)
+    g.tx_delay_table = _host(geom.d_txdelay, keep)
+    g.tx_apo_table = _host(geom.d_txapo, keep)
+    g.rx_apo_table = _host(geom.d_rxapo, keep)
+    g.pixel_phase = _host(geom.d_phase, keep)
+    if library_tiles:
+        g.tile_pixels, g.n_tiles = None, 0
+    else:
+        t = np.ascontiguousarray(geom.tiles, np.int32)
+        keep.append(t)
+        g.tile_pixels, g.n_tiles = t.ctypes.data, t.shape[0]
+    d.geometry = g
+    d.pixel_grid[0], d.pixel_grid[1], d.pixel_grid[2] = pixel_grid(geom.scan)
+    d.L, d.F = int(L), int(F)
+    d.storage, d.is_complex = STORE[Precision(precision)], int(bool(is_complex))
+    d.dimension, d.epilogue = int(dimension), int(bool(epilogue))
+    return d, keep
+
+
+def library_tiles(geom: FastGeometry, L: int = 1024) -> np.ndarray:
+    """The tile map the library plans for a geometry (``ustb_plan_tiles_host``; no GPU
+    needed), as an int32 array [n_tiles, TILE] with -1 for idle lanes."""
+    d, keep = plan_desc(geom, L, Precision.fp32, True, Dimension.both)
+    n = int(_lib.lib().ustb_plan_tiles_host(ctypes.addressof(d), None, 0))
+    if n < 0:
+        _lib.check(-n)
+    out = np.empty((n, TILE), np.int32)
+    got = int(_lib.lib().ustb_plan_tiles_host(ctypes.addressof(d), out.ctypes.data, n))
+    assert got == n
+    return out
+
+
 class Plan:
     """A resident plan built from a ``FastGeometry`` (its arrays are read back to the
     host and handed to ``ustb_plan_create``, which copies them to the device).
@@ -53,29 +94,8 @@ class Plan:
 
     def __init__(self, geom: FastGeometry, L: int, precision: Precision, is_complex: bool,
                  dimension=Dimension.both, F: int = 1, epilogue: bool = False, library_tiles: bool = True):
-        keep = []
-        d = CPlanDesc()
-        g = CGeometry()
-        ctypes.pointer(g)[0] = geom.c  # copy the scalar fields
-        g.element_xyz = _host(geom.d_el, keep)
-        g.pixel_xyz = _host(geom.d_px, keep)
-        g.waves = _host(geom.d_waves, keep)
-        g.tx_delay_table = _host(geom.d_txdelay, keep)
-        g.tx_apo_table = _host(geom.d_txapo, keep)
-        g.rx_apo_table = _host(geom.d_rxapo, keep)
-        g.pixel_phase = _host(geom.d_phase, keep)
-        if library_tiles:
-            g.tile_pixels, g.n_tiles = None, 0
-        else:
-            t = np.ascontiguousarray(geom.tiles, np.int32)
-            keep.append(t)
-            g.tile_pixels, g.n_tiles = t.ctypes.data, t.shape[0]
-        d.geometry = g
-        d.pixel_grid[0], d.pixel_grid[1], d.pixel_grid[2] = pixel_grid(geom.scan)
-        d.L, d.F = int(L), int(F)
+        d, keep = plan_desc(geom, L, precision, is_complex, dimension, F, epilogue, library_tiles)
         self.precision = Precision(precision)
-        d.storage, d.is_complex = STORE[self.precision], int(bool(is_complex))
-        d.dimension, d.epilogue = int(dimension), int(bool(epilogue))
         self.P, self.N, self.W, self.F, self.L = geom.P, geom.N, geom.W, int(F), int(L)
         self.is_complex, self.dimension, self.epilogue = bool(is_complex), int(dimension), bool(epilogue)
         self.device = geom.device
