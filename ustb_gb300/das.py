@@ -19,6 +19,7 @@ MATLAB shape [P, N|1, W|1, F] (see ``kernels.to_matlab_order``).
 """
 from __future__ import annotations
 
+import hashlib
 import math
 import time
 
@@ -91,6 +92,43 @@ class DAS:
         self.rf_mode = "analytic"  # "analytic" (das.m semantics) | "real" (real RF in, real out)
         self.epilogue = False      # fast engine, dimension.transmit: also CF / simplified-DMAS
         self.epilogue_outputs = None
+        # the last geometry on the device (tables or fast-path geometry) and the content
+        # key it was built from: go() on a new frame of the same acquisition reuses it
+        self._geometry = (None, None)
+
+    # -- geometry cache ---------------------------------------------------------
+    def geometry_key(self, engine: str, dev) -> bytes:
+        """Digest of everything the delays, apodizations and phase depend on: probe and
+        pixel positions, the waves, acquisition scalars, delay-model settings and both
+        apodizations.  Equal keys mean equal tables (das.m:91-209, 306-309)."""
+        cd, scan = self.channel_data, self.scan
+        h = hashlib.blake2b(digest_size=20)
+        add = lambda *v: h.update(repr(v).encode())
+        arr = lambda a: h.update(np.ascontiguousarray(np.asarray(a, np.float64)).tobytes())
+        add(engine, str(dev), type(scan).__name__, scan.N_pixels, cd.probe.N_elements, len(cd.sequence))
+        arr(cd.probe.xyz)
+        arr(scan.xyz)
+        arr(np.atleast_1d(np.asarray(scan.reference_distance, np.float64)))
+        for w in cd.sequence:
+            add(int(w.wavefront), w.source.distance, w.source.azimuth, w.source.elevation, w.origin.distance,
+                w.origin.azimuth, w.origin.elevation, w.delay, w.sound_speed)
+        add(float(cd.sampling_frequency), float(cd.initial_time), float(cd.modulation_frequency),
+            float(cd.sound_speed), float(self.lens_delay), int(self.spherical_transmit_delay_model),
+            float(self.pw_margin), float(self.blending_power))
+        for a in (self.receive_apodization, self.transmit_apodization):
+            o = a.origin
+            add(int(a.window), a.f_number, a.tilt, a.minimum_aperture, a.maximum_aperture, a.grating_lobe_angle,
+                a.MLA, a.MLA_overlap, None if o is None else (o.distance, o.azimuth, o.elevation))
+            if a.apodization_vector is not None:
+                arr(a.apodization_vector)
+        return h.digest()
+
+    def _cached(self, engine: str, dev, build):
+        key = self.geometry_key(engine, dev)
+        if self._geometry[0] != key:
+            self._geometry = (None, None)  # release the old one first
+            self._geometry = (key, build())
+        return self._geometry[1]
 
     # -- tables ---------------------------------------------------------------
     def tables(self):
@@ -126,14 +164,20 @@ class DAS:
         t0 = float(np.float32(cd.initial_time))
         fd = float(np.float32(cd.modulation_frequency))
         w0 = 2 * math.pi * fd
-        tx_apo, rx_apo, tx_delay, rx_delay = self.tables()
-        ch = self._channels(dev, w0)
         T = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
+
+        def build():
+            tx_apo, rx_apo, tx_delay, rx_delay = self.tables()
+            ph = None
+            if abs(w0) > np.finfo(np.float64).eps:
+                ph = torch.from_numpy(self.pixel_phase().astype(np.complex64)).to(dev)
+            return (T(tx_apo), T(rx_apo), T(tx_delay), T(rx_delay), ph, tx_delay, rx_delay)
+
+        d_txa, d_rxa, d_txd, d_rxd, ph, self.transmit_delay, self.receive_delay = self._cached("table", dev, build)
+        ch = self._channels(dev, w0)
         t_start = time.perf_counter()
-        out = kernels.das_table_f32(ch, fs, t0, T(tx_apo), T(rx_apo), T(tx_delay), T(rx_delay),
-                                    fd, self.dimension)
-        if abs(w0) > np.finfo(np.float64).eps:
-            ph = torch.from_numpy(self.pixel_phase().astype(np.complex64)).to(dev)
+        out = kernels.das_table_f32(ch, fs, t0, d_txa, d_rxa, d_txd, d_rxd, fd, self.dimension)
+        if ph is not None:
             kernels.apply_pixel_phase(out, ph)
         torch.cuda.synchronize(dev)
         self.elapsed_time = time.perf_counter() - t_start
@@ -172,7 +216,7 @@ class DAS:
         dev = torch.device("cuda", int(self.gpu_id))
         fd = float(np.float32(cd.modulation_frequency))
         ch = self._channels(dev, 2 * math.pi * fd)
-        geom = self.fast_geometry(dev)
+        geom = self._cached("fast", dev, lambda: self.fast_geometry(dev))
         prec = Precision(int(self.precision))
         t_start = time.perf_counter()
         st = fast.convert_channels(ch, prec)
