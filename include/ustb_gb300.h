@@ -422,6 +422,18 @@ int ustb_scan_convert(const void* data, int32_t is_complex, int32_t compression,
                       int64_t size_z, float x0, float dx, float z0, float dz, void* stream);
 
 /*
+ * Coherence factor of a kept cube (+postprocess/coherence_factor.m:100-135): over the
+ * channels (dimension USTB_DIM_RECEIVE), the waves (USTB_DIM_TRANSMIT) or both
+ * (USTB_DIM_BOTH) of cube [P, N, W, F] (complex single, pixel fastest):
+ * cf = |sum s|^2 / sum |s|^2 / M (NaN -> 0) and image = cf * sum s, both [P, J] with J
+ * the remaining dimensions in order (W*F, N*F or F).  active_count: [P] counts M (the
+ * reference's M = elements with apodization > active_element_criterium), or NULL for
+ * M = the number of terms summed (the Python port's rule).  cf or image may be NULL.
+ */
+int ustb_coherence_factor(const void* cube, int64_t P, int64_t N, int64_t W, int64_t F, int32_t dimension,
+                          const float* active_count, float* cf, void* image, void* stream);
+
+/*
  * Phase coherence factor on a kept cube (+postprocess/phase_coherence_factor.m:64-129):
  * cube [F][K][P] complex single (pixel fastest: the channels of a dimension.transmit
  * result, or the waves of a dimension.receive one), weights [K][P] (the apodization

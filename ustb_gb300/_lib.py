@@ -54,6 +54,7 @@ SIGNATURES = {
     "ustb_phase_coherence": (ctypes.c_int, [vp, i64, i64, i64, vp, f32, f32, vp, vp, vp, vp]),
     "ustb_generalized_coherence": (ctypes.c_int, [vp, i64, i64, i64, i32, vp, vp, vp]),
     "ustb_capon": (ctypes.c_int, [vp, vp, i64, i64, i64, i64, f32, i32, f32, f32, i32, vp, vp]),
+    "ustb_coherence_factor": (ctypes.c_int, [vp, i64, i64, i64, i64, i32, vp, vp, vp, vp]),
     "ustb_fir_depth": (ctypes.c_int, [vp, vp, i64, i64, vp, i32, i32, vp]),
 }
 

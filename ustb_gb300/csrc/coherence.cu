@@ -208,6 +208,36 @@ unsigned grid_for(int64_t total) {  // CTAs of kPix pixels
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + kPix - 1) / kPix, (int64_t)std::max(sms, 1) * 32));
 }
 
+// Coherence factor over the channels, the waves or both of a kept cube [P, N, W, F]
+// (pixel fastest), +postprocess/coherence_factor.m:100-135:
+//   CF = |sum s|^2 / sum |s|^2 * (1 / M)  (NaN -> 0),  image = CF * sum s,
+// M = the count of active units per pixel given by the caller, or the number summed
+// (the reference's Python CoherenceFactor, python/src/ustb/postprocess/coherence_factor.py:29-47).
+// One thread per (pixel, remaining index); a warp reads 32 consecutive pixels.
+__global__ void __launch_bounds__(kThreads) cf_kernel(const float2* __restrict__ cube, const float* __restrict__ M,
+                                                      int64_t P, int64_t K, int64_t S, int64_t J0, int64_t B0,
+                                                      int64_t B1, int64_t pblocks, float* __restrict__ cf,
+                                                      float2* __restrict__ img) {
+    const int64_t j = blockIdx.x / pblocks;
+    const int64_t p = (blockIdx.x - j * pblocks) * kThreads + threadIdx.x;
+    if (p >= P) return;
+    const int64_t j1 = j / J0, j0 = j - j1 * J0;
+    const float2* x = cube + j0 * B0 + j1 * B1 + p;
+    float2 sum = make_float2(0.f, 0.f);
+    float e = 0.f;
+    for (int64_t k = 0; k < K; ++k) {
+        const float2 v = __ldg(x + k * S);
+        sum.x += v.x;
+        sum.y += v.y;
+        e = fmaf(v.x, v.x, fmaf(v.y, v.y, e));
+    }
+    const float m = M ? __ldg(M + p) : (float)K;
+    float c = (sum.x * sum.x + sum.y * sum.y) / e * (1.f / m);
+    if (c != c) c = 0.f;  // NaN -> 0 (coherence_factor.m:132)
+    if (cf) cf[p + P * j] = c;
+    if (img) img[p + P * j] = make_float2(c * sum.x, c * sum.y);
+}
+
 }  // namespace
 
 extern "C" int ustb_phase_coherence(const void* cube, int64_t P, int64_t K, int64_t F, const float* weights,
@@ -259,6 +289,32 @@ extern "C" int ustb_generalized_coherence(const void* cube, int64_t P, int64_t K
         case 13: gcf_kernel<13><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
         default: gcf_kernel<15><<<grid, kThreads, smem, s>>>(c, P, K, F, bins, gcf, im); break;
     }
+    USTB_CUDA(cudaGetLastError());
+    return USTB_OK;
+}
+
+extern "C" int ustb_coherence_factor(const void* cube, int64_t P, int64_t N, int64_t W, int64_t F, int32_t dimension,
+                                     const float* active_count, float* cf, void* image, void* stream) {
+    ustb::clear_error();
+    USTB_REQUIRE(dimension == USTB_DIM_RECEIVE || dimension == USTB_DIM_TRANSMIT || dimension == USTB_DIM_BOTH,
+                 USTB_E_ARG, "dimension must be receive (1), transmit (2) or both (3), got %d", (int)dimension);
+    USTB_REQUIRE(P >= 0 && N >= 0 && W >= 0 && F >= 0, USTB_E_SHAPE, "negative size");
+    int64_t K, S, J0, B0, B1;
+    if (dimension == USTB_DIM_RECEIVE) {  // over channels; remaining (wave, frame)
+        K = N; S = P; J0 = W * F; B0 = P * N; B1 = 0;
+    } else if (dimension == USTB_DIM_TRANSMIT) {  // over waves; remaining (channel, frame)
+        K = W; S = P * N; J0 = N; B0 = P; B1 = P * N * W;
+    } else {  // over both; remaining frames
+        K = N * W; S = P; J0 = F; B0 = P * N * W; B1 = 0;
+    }
+    const int64_t J = (dimension == USTB_DIM_RECEIVE) ? W * F : (dimension == USTB_DIM_TRANSMIT ? N * F : F);
+    if (P == 0 || J == 0) return USTB_OK;
+    USTB_REQUIRE(cube && (cf || image), USTB_E_ARG, "NULL pointer");
+    const int64_t pblocks = (P + kThreads - 1) / kThreads;
+    USTB_REQUIRE(pblocks * J <= INT32_MAX, USTB_E_SHAPE, "too many pixels x remaining slices");
+    cf_kernel<<<(unsigned)(pblocks * J), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2*>(cube), active_count, P, K, S, J0, B0, B1, pblocks, cf,
+        static_cast<float2*>(image));
     USTB_CUDA(cudaGetLastError());
     return USTB_OK;
 }

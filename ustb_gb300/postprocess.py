@@ -1,5 +1,6 @@
 """Post-DAS steps: the follow-up of the fused coherence-factor / simplified-DMAS
-epilogue, and the phase / generalized coherence factors on a kept cube.
+epilogue, and the coherence, phase-coherence and generalized coherence factors and
+Capon's minimum variance on a kept cube.
 
 ``simplified_dmas_image`` completes +postprocess/simplified_delay_multiply_and_sum.m
 on a linear scan: the per-pixel value ((sum sign(s) sqrt|s|)^2 - sum |s|)/2
@@ -122,6 +123,86 @@ def simplified_dmas_image(sdmas: torch.Tensor, nz: int, nx: int, z_step: float, 
     y = sdmas.reshape(-1, nx, nz).to(torch.float32)
     filt = fir_depth(y.reshape(-1, nz), taps).reshape(-1, nx, nz)
     return hilbert_depth(filt).reshape(sdmas.shape[0], -1)
+
+
+def coherence_factor(cube: torch.Tensor, dimension, active_count: Optional[torch.Tensor] = None):
+    """Coherence factor (+postprocess/coherence_factor.m:100-135) of an ABI cube
+    (F, W, N, P) complex64 over the channels (Dimension.receive), the waves
+    (Dimension.transmit) or both (``ustb_coherence_factor``).  ``active_count``: (P,)
+    counts M of active units per pixel (the MATLAB rule), or None for M = the number
+    summed (the Python port's rule).  Returns dict of 'CF' (float32) and 'image'
+    (complex64), each (F, W, 1, P) / (F, 1, N, P) / (F, 1, 1, P) in the ABI layout."""
+    from .enums import Dimension
+
+    if cube.dim() != 4 or not cube.is_complex():
+        raise TypeError("cube must be a complex (F, W, N, P) tensor")
+    c = cube.to(torch.complex64).contiguous()
+    F, W, N, P = c.shape
+    d = int(dimension)
+    shape = {int(Dimension.receive): (F, W, 1, P), int(Dimension.transmit): (F, 1, N, P),
+             int(Dimension.both): (F, 1, 1, P)}.get(d)
+    if shape is None:
+        raise ValueError("dimension must be receive, transmit or both")
+    dev = c.device
+    m = None if active_count is None else active_count.to(device=dev, dtype=torch.float32).reshape(P).contiguous()
+    out = {"CF": torch.empty(shape, dtype=torch.float32, device=dev),
+           "image": torch.empty(shape, dtype=torch.complex64, device=dev)}
+    with torch.cuda.device(dev):
+        _lib.call("ustb_coherence_factor", c.data_ptr(), P, N, W, F, d, 0 if m is None else m.data_ptr(),
+                  out["CF"].data_ptr(), out["image"].data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+    return out
+
+
+class CoherenceFactor:
+    """postprocess.coherence_factor: ``input`` is BeamformedData whose ``data`` is the
+    channel / wave cube [P, N, W, F] (MATLAB order, complex; a device tensor or an
+    array); ``go()`` returns BeamformedData of CF * coherent sum, with the factor in
+    ``CF``.  M per pixel follows coherence_factor.m:100-126 when the apodization
+    tables are set (``receive_apodization`` [P, N], ``transmit_apodization`` [P, W]:
+    units with apodization above ``active_element_criterium``), else the number of
+    terms summed, as python/src/ustb/postprocess/coherence_factor.py does."""
+
+    def __init__(self):
+        from .enums import Dimension
+
+        self.input = None
+        self.dimension = Dimension.both
+        self.active_element_criterium = 0.16
+        self.receive_apodization = None
+        self.transmit_apodization = None
+        self.device = torch.device("cuda", 0)
+        self.CF = None
+
+    def _active_count(self, P: int):
+        from .enums import Dimension
+
+        thr = float(self.active_element_criterium)
+        rx, tx = self.receive_apodization, self.transmit_apodization
+        t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=self.device).reshape(P, -1)
+        d = int(self.dimension)
+        if d == int(Dimension.receive) and rx is not None:
+            return (t(rx) > thr).sum(dim=1).float()
+        if d == int(Dimension.transmit) and tx is not None:
+            return (t(tx) > thr).sum(dim=1).float()
+        if d == int(Dimension.both) and rx is not None and tx is not None:
+            a, b = t(tx), t(rx)
+            m = torch.empty(P, dtype=torch.float32, device=self.device)
+            for i in range(0, P, 2048):  # blocks of pixels, as the reference does (:103-114)
+                m[i:i + 2048] = ((a[i:i + 2048, None, :] * b[i:i + 2048, :, None]) > thr).sum(dim=(1, 2)).float()
+            return m
+        return None
+
+    def go(self):
+        from .kernels import to_matlab_order
+        from .uff import BeamformedData
+
+        data = self.input.data if torch.is_tensor(self.input.data) else torch.as_tensor(np.asarray(self.input.data))
+        while data.dim() < 4:
+            data = data.unsqueeze(-1)
+        cube = data.to(self.device).permute(3, 2, 1, 0).contiguous()  # [P,N,W,F] -> ABI (F, W, N, P)
+        out = coherence_factor(cube, self.dimension, self._active_count(cube.shape[-1]))
+        self.CF = BeamformedData(self.input.scan, to_matlab_order(out["CF"]))
+        return BeamformedData(self.input.scan, to_matlab_order(out["image"]))
 
 
 def _cube_fkp(cube: torch.Tensor) -> torch.Tensor:
