@@ -136,3 +136,16 @@ def test_zero_phase_short_trace_is_a_shape_error(cuda_dev):
     with pytest.raises(UstbError) as e:
         preprocess.demodulate(x, 20e6, 0.0, 4e6, b, 1, zero_phase=True)
     assert e.value.code == 2  # USTB_E_SHAPE
+
+
+def test_fast_demodulation_zero_phase_switch(cuda_dev):
+    """FastDemodulation(zero_phase=True) is the Python port's variant."""
+    rf = GOLDEN["default_dec/rf"]
+    fs, t0, fc, fds = GOLDEN["default_dec/params"]
+    a = preprocess.FastDemodulation()
+    a.input, a.modulation_frequency, a.zero_phase, a.device = _CD(rf.astype(np.float32), fs, t0).cd, fc, True, cuda_dev
+    b = preprocess.ZeroPhaseDemodulation()
+    b.input, b.modulation_frequency, b.device = _CD(rf.astype(np.float32), fs, t0).cd, fc, cuda_dev
+    oa, ob = a.go(), b.go()
+    assert torch.equal(oa.data, ob.data)
+    assert oa.sampling_frequency == ob.sampling_frequency and oa.initial_time == ob.initial_time

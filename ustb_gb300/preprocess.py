@@ -94,7 +94,9 @@ class FastDemodulation:
     power spectrum when empty), optionally ``downsample_frequency`` (default
     2 * modulation_frequency, :87-91) and ``lowpass_frequency_vector``; ``go()``
     returns IQ ChannelData whose ``data`` is a complex64 [L', N, W, F] view of
-    device memory."""
+    device memory.  ``zero_phase = True`` gives the reference's Python port instead
+    (``ZeroPhaseDemodulation``: filtfilt, t0 kept, its own default decimation).
+    """
 
     def __init__(self):
         self.input: Optional[ChannelData] = None
@@ -103,12 +105,20 @@ class FastDemodulation:
         self.lowpass_frequency_vector = (0.5, 1.0)
         self.precision = Precision.fp32
         self.device = torch.device("cuda", 0)
+        self.zero_phase = False
 
     @property
     def b(self) -> np.ndarray:
         return lowpass_taps(self.modulation_frequency, self.input.sampling_frequency, self.lowpass_frequency_vector)
 
     def go(self) -> ChannelData:
+        if self.zero_phase:
+            z = ZeroPhaseDemodulation()
+            z.input, z.modulation_frequency = self.input, self.modulation_frequency
+            z.downsample_frequency = self.downsample_frequency
+            z.lowpass_frequency_vector = list(self.lowpass_frequency_vector)
+            z.precision, z.device = self.precision, self.device
+            return z.go()
         cd = self.input
         if self.modulation_frequency is None:
             raise ValueError("set modulation_frequency (the centre frequency of the RF data)")
