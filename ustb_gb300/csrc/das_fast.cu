@@ -651,8 +651,8 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     if constexpr (ORDER_A) {
         int cur = -1;  // current wave chunk
         auto zero_chunks = [&](int from, int to) {  // receive mode: skipped chunks are zero
-            if (MODE != USTB_DIM_RECEIVE) return;
-            for (int w = from * KW; w < min(to * KW, (int)W); ++w) store_cube(p + A.w_f * w + A.f_f * f, zero2);
+            if constexpr (MODE == USTB_DIM_RECEIVE)
+                for (int w = from * KW; w < min(to * KW, (int)W); ++w) store_cube(p + A.w_f * w + A.f_f * f, zero2);
         };
         auto finish_chunk = [&]() {
             const int w0 = cur * KW;
@@ -730,13 +730,13 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         }
         int cur = -1;  // current channel group
         auto zero_groups = [&](int from, int to) {
-            if (MODE != USTB_DIM_TRANSMIT) return;
-            for (int n = from * CG; n < min(to * CG, (int)N); ++n) store_cube(p + A.rx_f * n + A.f_f * f, zero2);
+            if constexpr (MODE == USTB_DIM_TRANSMIT)
+                for (int n = from * CG; n < min(to * CG, (int)N); ++n) store_cube(p + A.rx_f * n + A.f_f * f, zero2);
         };
         auto finish_group = [&]() {
+            if constexpr (MODE != USTB_DIM_TRANSMIT) return;
             const int n0 = cur * CG;
             const int cg = min(CG, (int)N - n0);
-            if (MODE != USTB_DIM_TRANSMIT) return;
 #pragma unroll
             for (int c = 0; c < CG; ++c) {
                 if (c >= cg) continue;
