@@ -121,3 +121,23 @@ def test_plan_descriptor_checks_without_gpu(lib_path):
     d.epilogue = 0
     waves[0].kind = 3  # table wave without a table
     assert h.ustb_plan_create(ctypes.byref(d), ctypes.byref(out)) == 1 and b"tx_delay_table" in h.ustb_last_error()
+
+
+def test_kernel_entry_argument_errors_without_gpu(lib_path):
+    """Argument checks of the kernels around the beamformer, before any CUDA call."""
+    from ustb_gb300 import _lib
+
+    h = _lib.lib()
+    # coherence factor: only receive / transmit / both; empty input is a no-op
+    assert h.ustb_coherence_factor(None, 4, 2, 2, 1, 0, None, None, None, None) == 1
+    assert b"dimension" in h.ustb_last_error()
+    assert h.ustb_coherence_factor(None, 0, 2, 2, 1, 3, None, None, None, None) == 0
+    assert h.ustb_coherence_factor(None, 4, 2, 2, 1, 3, None, None, None, None) == 1  # NULL cube
+    # zero-phase demodulation: the trace must outlast filtfilt's padding of 3 * ntaps
+    assert h.ustb_demodulate_filtfilt(None, 0, None, 0, 150, 1, 20e6, 0.0, 4e6, 1, None, 65, 1.0, None) == 2
+    assert b"padding" in h.ustb_last_error()
+    assert h.ustb_demodulate_filtfilt(None, 0, None, 0, 300, 0, 20e6, 0.0, 4e6, 1, None, 65, 1.0, None) == 0
+    assert h.ustb_demodulate_filtfilt(None, 0, None, 0, 300, 1, 20e6, 0.0, 4e6, 0, None, 65, 1.0, None) == 1
+    # depth FIR
+    assert h.ustb_fir_depth(None, None, 16, 2, None, 0, 0, None) == 1
+    assert h.ustb_fir_depth(None, None, 16, 2, None, 5, -1, None) == 1
