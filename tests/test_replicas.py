@@ -44,7 +44,7 @@ def _worker(rank, world, port, out):
 
 def test_two_gloo_ranks_take_disjoint_requests_and_the_slowest_time():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this multi-threaded process
         out = m.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
