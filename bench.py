@@ -191,6 +191,62 @@ def cpu_reference(ch_np, fs, t0, fd, tabs, dim, target_s=12.0, steps=1):
                       f"oracle/das_port.c oracle_das_f32 (bit-identical to das_c) on {threads} threads"}
 
 
+def fp64_subset_reference(wl, das, ch_matlab, sel):
+    """The FP64 oracle (das_c's formula in double) on a pixel subset, with double tables
+    from the host geometry code, and the das.m phase epilogue."""
+    from oracle import oracle as O
+    from ustb_gb300 import geometry
+    from ustb_gb300.uff import Scan, SectorScan
+
+    cd = wl.channel_data
+    sub = Scan(wl.scan.x[sel], wl.scan.y[sel], wl.scan.z[sel])
+    txa = das.transmit_apodization.wave_apodization(cd.sequence, wl.scan)[sel]
+    if isinstance(wl.scan, SectorScan):  # aperture centred on the sector origin: full-scan table
+        rxa = das.receive_apodization.aperture_apodization(cd.probe, wl.scan)[sel]
+    else:
+        rxa = das.receive_apodization.aperture_apodization(cd.probe, sub)
+    txd = geometry.transmit_delay(cd.sequence, wl.scan)[sel]
+    rxd = geometry.receive_delay(cd.probe, sub, cd.sound_speed)
+    ref = O.das_f64(ch_matlab.astype(np.complex128), cd.sampling_frequency, cd.initial_time, txa, rxa, txd, rxd,
+                    cd.modulation_frequency, int(wl.dimension))
+    if abs(cd.modulation_frequency) > 0:
+        ph = np.exp(-1j * 4 * np.pi * cd.modulation_frequency * np.asarray(wl.scan.reference_distance)[sel]
+                    / cd.sound_speed)
+        ref = ref * ph.reshape((-1,) + (1,) * (ref.ndim - 1))
+    return ref
+
+
+def headline_parity(wl, das, ch, tabs, phase, fast_step, st32, st16, table_step, out_t, torch, n_pix=2000):
+    """Measured relative L2 of the headline outputs on a seeded pixel subset: the table
+    kernel and the FP32 fast path against the das_c port (das.m's single-precision
+    tables, then the per-pixel phase), and both storages of the fast path against the
+    FP64 oracle."""
+    from oracle import oracle as O
+    from ustb_gb300 import kernels
+    from ustb_gb300.enums import Precision
+
+    cd = wl.channel_data
+    fs, t0, fd = (float(np.float32(cd.sampling_frequency)), float(np.float32(cd.initial_time)),
+                  float(np.float32(cd.modulation_frequency)))
+    sel = np.sort(np.random.default_rng(11).choice(wl.scan.N_pixels, n_pix, replace=False))
+    ch_np = kernels.to_matlab_order(ch).cpu().numpy()
+    ph = phase.cpu().numpy()[sel].reshape(-1, 1, 1, 1)
+    port = O.das_f32(ch_np, fs, t0, tabs[0][sel], tabs[1][sel], tabs[2][sel], tabs[3][sel], fd, 3,
+                     threads=os.cpu_count() or 1) * ph
+    f64 = fp64_subset_reference(wl, das, ch_np, sel)
+    table_step()
+    got_t = kernels.to_matlab_order(out_t).cpu().numpy()[sel]
+    got32 = kernels.to_matlab_order(fast_step(st32, Precision.fp32)()["cube"]).cpu().numpy()[sel]
+    got16 = kernels.to_matlab_order(fast_step(st16, Precision.fp16)()["cube"]).cpu().numpy()[sel]
+    rel = lambda a, b: float(f"{np.linalg.norm(a - b) / np.linalg.norm(b):.3g}")
+    return {"pixels": int(n_pix), "seed": 11,
+            "table_vs_das_c_port": rel(got_t, port),
+            "fast_fp32_vs_das_c_port": rel(got32, port),
+            "fast_fp32_vs_fp64_oracle": rel(got32, f64),
+            "fast_fp16_vs_fp64_oracle": rel(got16, f64),
+            "table_vs_fp64_oracle": rel(got_t, f64)}
+
+
 # ---------------------------------------------------------------------------
 def serving_mix(device, n_requests, seed, torch):
     """Served FP16 continuous batching vs plain single-request FP32 DAS on a seeded
@@ -306,23 +362,7 @@ def serving_mix(device, n_requests, seed, torch):
         job = next(j for j in jobs if j.key == k)
         cd = wl.channel_data
         sel = np.random.default_rng(0).choice(wl.scan.N_pixels, min(1500, wl.scan.N_pixels), replace=False)
-        from ustb_gb300.uff import Scan, SectorScan
-
-        sub = Scan(wl.scan.x[sel], wl.scan.y[sel], wl.scan.z[sel])
-        txa = das.transmit_apodization.wave_apodization(cd.sequence, wl.scan)[sel]
-        if isinstance(wl.scan, SectorScan):  # aperture centred on the sector origin: full-scan table
-            rxa = das.receive_apodization.aperture_apodization(cd.probe, wl.scan)[sel]
-        else:
-            rxa = das.receive_apodization.aperture_apodization(cd.probe, sub)
-        txd = geometry.transmit_delay(cd.sequence, wl.scan)[sel]
-        rxd = geometry.receive_delay(cd.probe, sub, cd.sound_speed)
-        chn = kernels.to_matlab_order(ch).cpu().numpy().astype(np.complex128)
-        ref = O.das_f64(chn, cd.sampling_frequency, cd.initial_time, txa, rxa, txd, rxd,
-                        cd.modulation_frequency, int(wl.dimension))
-        if abs(cd.modulation_frequency) > 0:
-            ph = np.exp(-1j * 4 * np.pi * cd.modulation_frequency * np.asarray(wl.scan.reference_distance)[sel]
-                        / cd.sound_speed)
-            ref = ref * ph.reshape((-1,) + (1,) * (ref.ndim - 1))
+        ref = fp64_subset_reference(wl, das, kernels.to_matlab_order(ch).cpu().numpy(), sel)
         if job.epilogue:
             got = job.outputs["das"].cpu().numpy()[0][sel]
             want = ref[:, :, 0, 0].sum(axis=1)
@@ -577,6 +617,8 @@ def main():
     if pipe.overflowed():
         raise RuntimeError("fast path flagged a window overflow in the end-to-end run")
 
+    parity = headline_parity(wl, das, ch, tabs, phase, fast_step, st32, st16, table_step, out_t, torch)
+
     serving = None
     if world == 1 and not args.no_serving:
         serving = serving_mix(dev, args.serving_requests, 11, torch)
@@ -610,7 +652,8 @@ def main():
                              "value": round(units / statistics.mean(ms16) / 1e6, 2)},
             "das_c_exact_table_kernel": {"ms_per_step": round(statistics.mean(mst), 4),
                                          "value": round(units / statistics.mean(mst) / 1e6, 2),
-                                         "parity": "<= 1e-5 rel-L2 vs das_c"},
+                                         "rel_l2_vs_das_c_port": parity["table_vs_das_c_port"]},
+            "parity": parity,
             "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
         },
         "roofline": {

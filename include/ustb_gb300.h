@@ -82,7 +82,9 @@ int ustb_das_table_f32(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
  * Host-pointer form of ustb_das_table_f32 (the MEX gateway's call).
  * Replaces the same das.m:251-259 call, and das.m:262-271 (mex.das_cuda with
  * int32 gpu_id) when `device` is given.  Copies the inputs to `device`, runs
- * the kernel, copies the result into `out` and synchronises.
+ * the kernel, copies the result into `out` and synchronises.  The calling
+ * thread's current device is restored before the call returns.  Sizes whose
+ * byte counts overflow 64 bits are rejected with USTB_E_SHAPE.
  */
 int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64_t L, int64_t N, int64_t W,
                             int64_t F, float fs, float t0, const float* apo_tx,
@@ -105,8 +107,10 @@ int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64_t L, int64
  * buffers (channel data, the four tables and the output, each rounded up to
  * 256 bytes) come from one static device array of USTB_NOALLOC_SCRATCH_BYTES
  * that every GPU which loads this library holds until the process exits.
- * Requests that need more are rejected with USTB_E_SHAPE before any copy.
- * The call makes no cudaMalloc/cudaFree and uses the per-thread default stream.
+ * Requests that need more (including sizes whose byte counts overflow 64 bits)
+ * are rejected with USTB_E_SHAPE before any copy.  The call makes no
+ * cudaMalloc/cudaFree, uses the per-thread default stream and restores the
+ * calling thread's current device before it returns.
  * Its first call on a device looks up the array's device address (set-up, once
  * per device); make that first call before any stream capture on that device.
  * All calls share the one array and nothing in it is cleared (every byte used is

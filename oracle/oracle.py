@@ -68,13 +68,14 @@ _f64 = ctypes.c_double
 _ptr = ctypes.c_void_p
 
 
-def build() -> None:
-    """Compile the C restatement (and the reference das_c when its source exists)."""
+def build(reference: Optional[str] = None) -> None:
+    """Compile the C restatement, and the reference's own das_c from the checkout at
+    ``reference`` (or ``$USTB_REFERENCE_ROOT``) when one is given and holds its source."""
     import subprocess
 
     subprocess.check_call(["make", "-s", "-C", _HERE, "all"])
-    ref = os.environ.get("USTB_REFERENCE_ROOT", "/root/reference")
-    if os.path.isfile(os.path.join(ref, "+mex", "source", "das_c.cpp")):
+    ref = reference or os.environ.get("USTB_REFERENCE_ROOT")
+    if ref and os.path.isfile(os.path.join(ref, "+mex", "source", "das_c.cpp")):
         subprocess.check_call(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"])
 
 

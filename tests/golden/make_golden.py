@@ -4,7 +4,7 @@ Run in a container where the reference checkout is present (it is not needed
 afterwards; the fixtures are committed):
 
     make -C oracle ref                       # builds the reference das_c from source
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <reference checkout>
 
 Fixtures written:
 
@@ -291,8 +291,11 @@ def make_python_cf(out_path, reference_root):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("USTB_REFERENCE_ROOT"),
+                    help="the reference checkout (default: $USTB_REFERENCE_ROOT)")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("give --reference <reference checkout> or set USTB_REFERENCE_ROOT")
     make_das_c_cases(os.path.join(HERE, "das_c_cases.npz"))
     make_python_das(os.path.join(HERE, "python_das.npz"), a.reference)
     make_python_demod(os.path.join(HERE, "python_demod.npz"), a.reference)

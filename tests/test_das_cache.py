@@ -52,3 +52,21 @@ def test_go_reuses_device_geometry(cuda_dev, engine, prec):
     c = d.go().data
     assert d._geometry[1] is not geom  # rebuilt for the new scan
     assert not torch.equal(a, c)
+
+
+@pytest.mark.gpu
+def test_fixed_geometry_skips_the_key_until_invalidated(cuda_dev, monkeypatch):
+    wl = synth.config_iq_cpwc(device=cuda_dev, scale=0.15)
+    d = bench.build_das(wl)
+    d.engine, d.precision, d.gpu_id = "fast", Precision.fp16, cuda_dev.index or 0
+    a = d.go().data.clone()
+    geom = d._geometry[1]
+    d.geometry_fixed = True
+    calls = []
+    orig = type(d).geometry_key
+    monkeypatch.setattr(type(d), "geometry_key", lambda self, *a_: calls.append(1) or orig(self, *a_))
+    b = d.go().data
+    assert not calls and d._geometry[1] is geom and torch.equal(a, b)
+    d.invalidate()
+    d.go()
+    assert calls and d._geometry[1] is not geom

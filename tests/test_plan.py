@@ -47,3 +47,21 @@ def test_library_planner_on_a_pixel_list():
     for row in lt:
         b = scan.xyz[row[row >= 0]]
         assert len(b) == 1 or np.linalg.norm(b.max(0) - b.min(0)) <= limit * (1 + 1e-9)
+
+
+@pytest.mark.parametrize("what", ["pixel", "element"])
+def test_library_planner_rejects_non_finite_positions(what):
+    import ctypes
+
+    from ustb_gb300 import _lib
+    from ustb_gb300.enums import Precision
+    from ustb_gb300.plan import plan_desc
+
+    wl = synth.CONFIGS["iq_cpwc"](device="cpu", scale=0.1)
+    g = bench.build_das(wl).fast_geometry("cpu")
+    d, keep = plan_desc(g, 1024, Precision.fp32, True)
+    ptr = d.geometry.pixel_xyz if what == "pixel" else d.geometry.element_xyz
+    ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float))[4] = float("nan")
+    n = int(_lib.lib().ustb_plan_tiles_host(ctypes.addressof(d), None, 0))
+    assert n == -1  # USTB_E_ARG
+    assert b"non-finite" in _lib.lib().ustb_last_error()

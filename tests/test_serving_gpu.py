@@ -26,7 +26,8 @@ def rel(a, b):
 def workloads(cuda_dev):
     out = {}
     for name, fn in (("iq", synth.config_iq_cpwc), ("sector", synth.config_dw_sector),
-                     ("rf", synth.config_rf_plane_wave), ("sta", synth.config_sta)):
+                     ("rf", synth.config_rf_plane_wave), ("sta", synth.config_sta),
+                     ("m3d", synth.config_matrix_3d)):
         wl = fn(device=cuda_dev, scale=0.15)
         das = DAS()
         das.channel_data, das.scan, das.dimension = wl.channel_data, wl.scan, wl.dimension

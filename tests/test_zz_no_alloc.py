@@ -1,10 +1,13 @@
 """The allocation-free host entry point against the regular one.
 
 ustb_das_table_f32_host_noalloc serves callers that cannot allocate device
-memory while they run (latency-bound acquisition loops, processes whose GPU
-memory is owned by another allocator): it stages through a fixed static device
-array instead of cudaMalloc.  Its output must equal that of
-ustb_das_table_f32_host, call after call, since every call reuses the same array.
+memory while they run.  Examples are acquisition loops with a hard latency
+budget, where cudaMalloc may block or synchronise the device, and processes
+whose GPU memory belongs to another allocator.  It stages through a fixed static
+device array instead of calling cudaMalloc.  Its output must be bit-for-bit that
+of ustb_das_table_f32_host, call after call, because every call reuses the same
+array.  It must also match the reference das_c's own golden output, take no
+device memory, and leave the caller's current device as it was.
 This file is collected last on purpose.
 """
 import os
@@ -14,7 +17,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-5  # the table kernel's parity bar
+TOL = 1e-5  # the table kernel's parity bar against das_c
 
 
 def _case(golden_dir, name):
@@ -42,6 +45,10 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
 @pytest.mark.parametrize("dim", [0, 1, 2, 3])
 def test_noalloc_matches_regular_entry_two_calls_in_a_row(golden_dir, cuda_dev, dim):
     a = _case(golden_dir, "iq_small")
@@ -50,13 +57,37 @@ def test_noalloc_matches_regular_entry_two_calls_in_a_row(golden_dir, cuda_dev, 
     ref_b = _run("ustb_das_table_f32_host", b, dim)
     first = _run("ustb_das_table_f32_host_noalloc", a, dim)
     second = _run("ustb_das_table_f32_host_noalloc", a, dim)
-    assert _rel(first, ref_a) <= TOL
-    assert _rel(second, ref_a) <= TOL
+    # the same kernel on the same inputs: bit-for-bit the regular entry's result
+    assert np.array_equal(_bits(first), _bits(ref_a))
+    assert np.array_equal(_bits(second), _bits(ref_a))
+    # and within the parity bar of the reference das_c's own output
+    assert _rel(first, a[f"out_dim{dim}"]) <= TOL
     # a different request in between leaves nothing behind in the shared array
     other = _run("ustb_das_table_f32_host_noalloc", b, dim)
     again = _run("ustb_das_table_f32_host_noalloc", a, dim)
-    assert _rel(other, ref_b) <= TOL
-    assert _rel(again, ref_a) <= TOL
+    assert np.array_equal(_bits(other), _bits(ref_b))
+    assert _rel(other, b[f"out_dim{dim}"]) <= TOL
+    assert np.array_equal(_bits(again), _bits(ref_a))
+
+
+def test_noalloc_takes_no_device_memory_and_keeps_the_current_device(golden_dir, cuda_dev):
+    import torch
+
+    a = _case(golden_dir, "iq_small")
+    b = _case(golden_dir, "iq_long_delay")
+    for dim in range(4):  # warm-up: every kernel variant used below is loaded
+        _run("ustb_das_table_f32_host_noalloc", a, dim)
+        _run("ustb_das_table_f32_host_noalloc", b, dim)
+    torch.cuda.synchronize()
+    before = torch.cuda.mem_get_info(cuda_dev)[0]
+    cur = torch.cuda.current_device()
+    for _ in range(5):
+        for dim in range(4):
+            _run("ustb_das_table_f32_host_noalloc", a, dim)
+            _run("ustb_das_table_f32_host_noalloc", b, dim)
+        assert torch.cuda.current_device() == cur
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(cuda_dev)[0] == before
 
 
 def test_noalloc_rejects_requests_beyond_its_scratch(cuda_dev):
@@ -71,3 +102,10 @@ def test_noalloc_rejects_requests_beyond_its_scratch(cuda_dev):
                                            tiny.ctypes.data, 4, 0.0, 3, out.ctypes.data, 0)
     assert rc == 2
     assert b"scratch" in h.ustb_last_error()
+    # sizes whose byte counts wrap 64 bits are rejected too, not under-counted
+    big = 1 << 31
+    rc = h.ustb_das_table_f32_host_noalloc(tiny.ctypes.data, 1, big - 1, big, 1 << 20, 1, 20e6, 0.0,
+                                           tiny.ctypes.data, tiny.ctypes.data, tiny.ctypes.data,
+                                           tiny.ctypes.data, 4, 0.0, 3, out.ctypes.data, 0)
+    assert rc == 2
+    assert b"overflow" in h.ustb_last_error()

@@ -222,6 +222,61 @@ int check_table_args(const void* ch, int32_t ch_complex, int64_t L, int64_t N, i
     return USTB_OK;
 }
 
+// Byte counts of the host-pointer entries' device copies: channel data, one tx
+// table, one rx table and the output.  Every product is checked for overflow, so
+// a request whose sizes wrap 64 bits is rejected instead of under-allocated.
+struct StagingBytes {
+    size_t ch, tx, rx, out, total;
+};
+
+int staging_bytes(int32_t ch_complex, int64_t L, int64_t N, int64_t W, int64_t F, int64_t P, int32_t dim,
+                  StagingBytes& b) {
+    const uint64_t el = ch_complex ? 8 : 4;
+    uint64_t ch = 0, tx = 0, rx = 0, out = 0, t = 0;
+    const int64_t nk = (dim == USTB_DIM_NONE || dim == USTB_DIM_TRANSMIT) ? N : 1;
+    const int64_t wk = (dim == USTB_DIM_NONE || dim == USTB_DIM_RECEIVE) ? W : 1;
+    bool bad = __builtin_mul_overflow((uint64_t)L, (uint64_t)N, &t) || __builtin_mul_overflow(t, (uint64_t)W, &t) ||
+               __builtin_mul_overflow(t, (uint64_t)F, &t) || __builtin_mul_overflow(t, el, &ch);
+    bad = bad || __builtin_mul_overflow((uint64_t)P, (uint64_t)W, &t) || __builtin_mul_overflow(t, (uint64_t)4, &tx);
+    bad = bad || __builtin_mul_overflow((uint64_t)P, (uint64_t)N, &t) || __builtin_mul_overflow(t, (uint64_t)4, &rx);
+    bad = bad || __builtin_mul_overflow((uint64_t)P, (uint64_t)nk, &t) || __builtin_mul_overflow(t, (uint64_t)wk, &t) ||
+          __builtin_mul_overflow(t, (uint64_t)F, &t) || __builtin_mul_overflow(t, el, &out);
+    // each part is padded to 256 bytes; the sum of six padded parts must not wrap either
+    const uint64_t lim = (UINT64_MAX >> 4) - 256;
+    bad = bad || ch > lim || tx > lim || rx > lim || out > lim;
+    USTB_REQUIRE(!bad, USTB_E_SHAPE, "the request's byte counts overflow 64 bits (L=%lld N=%lld W=%lld F=%lld P=%lld)",
+                 (long long)L, (long long)N, (long long)W, (long long)F, (long long)P);
+    auto align = [](uint64_t v) { return (v + 255) & ~uint64_t(255); };
+    b.ch = (size_t)ch;
+    b.tx = (size_t)tx;
+    b.rx = (size_t)rx;
+    b.out = (size_t)out;
+    b.total = (size_t)(align(ch) + 2 * align(tx) + 2 * align(rx) + align(out));
+    return USTB_OK;
+}
+
+// Makes `device` current for the lifetime of the guard and then restores the
+// caller's current device, so the host-pointer entries leave the calling thread's
+// CUDA state as they found it.
+class DeviceGuard {
+public:
+    int enter(int device) {
+        USTB_CUDA(cudaGetDevice(&prev_));
+        if (prev_ != device) {
+            USTB_CUDA(cudaSetDevice(device));
+            restore_ = true;
+        }
+        return USTB_OK;
+    }
+    ~DeviceGuard() {
+        if (restore_) (void)cudaSetDevice(prev_);
+    }
+
+private:
+    int prev_ = 0;
+    bool restore_ = false;
+};
+
 }  // namespace
 
 extern "C" int ustb_das_table_f32(const void* ch, int32_t ch_complex, int64_t L, int64_t N,
@@ -269,16 +324,17 @@ extern "C" int ustb_das_table_f32_host(const void* ch, int32_t ch_complex, int64
     int rc = check_table_args(ch, ch_complex, L, N, W, F, fd, dimension, apo_tx, apo_rx, delay_tx,
                               delay_rx, P, out);
     if (rc) return rc;
-    USTB_CUDA(cudaSetDevice(device));
-    const size_t el = ch_complex ? 8 : 4;
-    const size_t ch_bytes = (size_t)(L * N * W * F) * el;
-    const size_t tx_bytes = (size_t)(P * W) * 4, rx_bytes = (size_t)(P * N) * 4;
-    const size_t out_bytes = (size_t)out_elems(dimension, P, N, W, F) * el;
+    StagingBytes sb;
+    rc = staging_bytes(ch_complex, L, N, W, F, P, dimension, sb);
+    if (rc) return rc;
+    DeviceGuard dg;
+    rc = dg.enter(device);
+    if (rc) return rc;
+    const size_t ch_bytes = sb.ch, tx_bytes = sb.tx, rx_bytes = sb.rx, out_bytes = sb.out, total = sb.total;
     cudaStream_t s;
     USTB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     char* buf = nullptr;
     auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
-    const size_t total = align(ch_bytes) + 2 * align(tx_bytes) + 2 * align(rx_bytes) + align(out_bytes);
     cudaError_t e = cudaMallocAsync((void**)&buf, total ? total : 256, s);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s);
@@ -353,17 +409,18 @@ extern "C" int ustb_das_table_f32_host_noalloc(const void* ch, int32_t ch_comple
     int rc = check_table_args(ch, ch_complex, L, N, W, F, fd, dimension, apo_tx, apo_rx, delay_tx,
                               delay_rx, P, out);
     if (rc) return rc;
-    const size_t el = ch_complex ? 8 : 4;
-    const size_t ch_bytes = (size_t)(L * N * W * F) * el;
-    const size_t tx_bytes = (size_t)(P * W) * 4, rx_bytes = (size_t)(P * N) * 4;
-    const size_t out_bytes = (size_t)out_elems(dimension, P, N, W, F) * el;
+    StagingBytes sb;
+    rc = staging_bytes(ch_complex, L, N, W, F, P, dimension, sb);
+    if (rc) return rc;
+    const size_t ch_bytes = sb.ch, tx_bytes = sb.tx, rx_bytes = sb.rx, out_bytes = sb.out, total = sb.total;
     auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
-    const size_t total = align(ch_bytes) + 2 * align(tx_bytes) + 2 * align(rx_bytes) + align(out_bytes);
     USTB_REQUIRE(total <= (size_t)USTB_NOALLOC_SCRATCH_BYTES, USTB_E_SHAPE,
                  "this request needs %zu bytes of device scratch; the allocation-free entry point has "
                  "%zu (USTB_NOALLOC_SCRATCH_BYTES): use ustb_das_table_f32_host or split the pixels",
                  total, (size_t)USTB_NOALLOC_SCRATCH_BYTES);
-    USTB_CUDA(cudaSetDevice(device));
+    DeviceGuard dg;
+    rc = dg.enter(device);
+    if (rc) return rc;
     void* scratch = nullptr;
     rc = noalloc_scratch(device, &scratch);
     if (rc) return rc;

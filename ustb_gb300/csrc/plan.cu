@@ -109,6 +109,10 @@ void split_boxes(const Pts& p, Box root, double limit, std::vector<std::vector<i
                 best = ax;
             }
         }
+        if (best < 0) {  // no axis with a finite extent to halve: keep the box whole
+            out.push_back(std::move(b.idx));
+            continue;
+        }
         const int64_t h = b.d[best] / 2;
         stack.push_back(sub_box(b, best, 0, h));
         stack.push_back(sub_box(b, best, h, b.d[best]));
@@ -305,6 +309,12 @@ static int plan_tiles(const ustb_plan_desc* d, std::vector<int32_t>& tiles, int6
     USTB_REQUIRE(!d->epilogue || (d->is_complex && d->dimension == USTB_DIM_TRANSMIT), USTB_E_ARG,
                  "the epilogue needs complex data and dimension.transmit");
     USTB_REQUIRE(h.fs > 0.f && h.sound_speed > 0.f, USTB_E_ARG, "fs and sound speed must be > 0");
+    for (int64_t i = 0; i < 3 * h.n_pixels; ++i)
+        USTB_REQUIRE(std::isfinite(h.pixel_xyz[i]), USTB_E_ARG, "pixel %lld has a non-finite coordinate",
+                     (long long)(i / 3));
+    for (int64_t i = 0; i < 3 * h.n_elements; ++i)
+        USTB_REQUIRE(std::isfinite(h.element_xyz[i]), USTB_E_ARG, "element %lld has a non-finite coordinate",
+                     (long long)(i / 3));
     bool tables = false;
     for (int64_t w = 0; w < h.n_waves; ++w) {
         USTB_REQUIRE(h.waves[w].kind >= 0 && h.waves[w].kind <= 3, USTB_E_ARG, "wave %lld: unknown kind",

@@ -95,6 +95,10 @@ class DAS:
         # the last geometry on the device (tables or fast-path geometry) and the content
         # key it was built from: go() on a new frame of the same acquisition reuses it
         self._geometry = (None, None)
+        # True: the caller promises the geometry is unchanged between go() calls, so a
+        # cached device geometry is reused without hashing the scan, probe and waves
+        # again (call invalidate() after changing any of them)
+        self.geometry_fixed = False
 
     # -- geometry cache ---------------------------------------------------------
     def geometry_key(self, engine: str, dev) -> bytes:
@@ -123,8 +127,14 @@ class DAS:
                 arr(a.apodization_vector)
         return h.digest()
 
+    def invalidate(self) -> None:
+        """Drop the cached device geometry; the next go() rebuilds it."""
+        self._geometry = (None, None)
+
     def _cached(self, engine: str, dev, build):
-        key = self.geometry_key(engine, dev)
+        if self.geometry_fixed and self._geometry[0] is not None and self._geometry[0][:2] == (engine, str(dev)):
+            return self._geometry[1]
+        key = (engine, str(dev), self.geometry_key(engine, dev))
         if self._geometry[0] != key:
             self._geometry = (None, None)  # release the old one first
             self._geometry = (key, build())
