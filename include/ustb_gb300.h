@@ -50,7 +50,7 @@ enum { USTB_DIM_NONE = 0, USTB_DIM_RECEIVE = 1, USTB_DIM_TRANSMIT = 2, USTB_DIM_
 const char* ustb_last_error(void);
 
 /* ABI version of this library (major*10000 + minor*100 + patch). */
-int ustb_abi_version(void); /* 10100: ustb_das_geometry.ctas_per_tile */
+int ustb_abi_version(void); /* 10200: ustb_das_geometry.stage_shape */
 
 /*
  * Plain single-precision DAS on precomputed delay/apodization tables: the
@@ -204,6 +204,10 @@ typedef struct {
     int32_t ctas_per_tile;       /* dimension.both, one launch per request: 1 or 2 CTAs per tile (two
                                     add partial sums over halves of the tile's work); 0 = the library
                                     picks 2 when there are fewer than 4 tiles per SM */
+    int32_t stage_shape;         /* (channel, wave) pairs per shared-memory stage and loop order:
+                                    1 = waves outer, 2 channels x 16 waves (dimension.both / receive);
+                                    2 = channels outer, 8 x 4; 3 = channels outer, 16 x 2
+                                    (dimension.both / transmit / none); 0 = the library's choice */
 } ustb_das_geometry;
 
 /* Outputs of ustb_das_fast (device pointers; unused ones NULL). */

@@ -46,6 +46,7 @@ constexpr int kSlot = 160;                      // entries per (channel, wave) w
 constexpr float kHalf = (float)(kSlot / 2 - 1);  // max relative delay of each component
 constexpr float kMagic = 8388608.0f;            // 2^23: floor via round-toward-zero add
 constexpr int kMagicBits = 0x4B000000;
+constexpr int kBothShape = 1;                   // dimension.both: channels outer, 8 x 4 stages
 
 struct Params {
     const void* entries;  // [F][W][N][Lp] interpolation entries (float4 complex, float2 real)
@@ -74,6 +75,7 @@ struct Params {
     int64_t rx_f, w_f, f_f;
     uint32_t* flags;
     int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list); 0 = auto
+    int shape;  // stage shape (Shape<> index)
 };
 
 // ---------------------------------------------------------------------------
@@ -173,23 +175,6 @@ __device__ __forceinline__ void dist_range(const Box& b, float x, float y, float
     }
     dmin = sqrtf(n2);
     dmax = sqrtf(f2);
-}
-
-// transmit delay (s) of one wave at one pixel
-__device__ __forceinline__ float tx_tau(const Params& A, const ustb_wave& wv, int64_t w, int64_t p,
-                                        float px, float py, float pz) {
-    switch (wv.kind) {
-        case USTB_WAVE_PLANE:
-            return __fdividef(px * wv.dir[0] + py * wv.dir[1] + pz * wv.dir[2], wv.sound_speed) - wv.delay;
-        case USTB_WAVE_SPHERICAL: {
-            const float dx = px - wv.src[0], dy = py - wv.src[1], dz = pz - wv.src[2];
-            const float d = sqrtf(dx * dx + dy * dy + dz * dz);
-            const float sg = pz < wv.src[2] ? -1.f : 1.f;
-            return __fdividef(sg * d + wv.offset, wv.sound_speed) - wv.delay;
-        }
-        case USTB_WAVE_TABLE: return A.tx_delay_tab ? __ldg(A.tx_delay_tab + w * A.P + p) : -wv.delay;
-        default: return -wv.delay;
-    }
 }
 
 // lower / upper bound of a wave's transmit delay (s) over the tile box
@@ -330,19 +315,72 @@ struct CtasPerSm {
     static constexpr int value = 1;  // 512 threads x 128 registers fill the register file
 };
 
-template <bool ORDER_A>
-struct StageShape {
-    static constexpr int CG = ORDER_A ? 2 : 8;   // channels per stage
-    static constexpr int KW = ORDER_A ? 16 : 4;  // waves per stage
-    static constexpr int NS = CG * KW;           // slots per stage
+// Stage shapes: a stage is CG channels x KW waves = 32 (channel, wave) slots.
+//   shape 0: waves outer (2 channels x 16 waves); per-wave accumulators, the
+//            receive geometry of a channel is formed once per 16-wave chunk
+//   shape 1: channels outer (8 channels x 4 waves); per-channel accumulators,
+//            the receive geometry is formed once per (pixel, channel) and the
+//            transmit geometry once per stage
+//   shape 2: channels outer (16 channels x 2 waves)
+// dimension.receive needs waves outer, dimension.transmit/none channels outer;
+// dimension.both runs with any of the three.
+template <int SHAPE>
+struct Shape;
+template <>
+struct Shape<0> {
+    static constexpr bool WAVES_OUTER = true;
+    static constexpr int CG = 2, KW = 16;
+};
+template <>
+struct Shape<1> {
+    static constexpr bool WAVES_OUTER = false;
+    static constexpr int CG = 8, KW = 4;
+};
+template <>
+struct Shape<2> {
+    static constexpr bool WAVES_OUTER = false;
+    static constexpr int CG = 16, KW = 2;
 };
 constexpr int kStageSlots = 32;
 
 // Shared memory of one CTA: two stage buffers of kStageSlots slots x kSlot entries,
-// then the per-tile tables (their size depends on N and W).
+// then the per-tile tables (their size depends on N, W and the stage shape).
 template <bool CPLX>
 constexpr size_t slot_buffer_bytes() {
     return (size_t)2 * kStageSlots * kSlot * (CPLX ? 16 : 8);
+}
+
+// Byte offsets of the per-tile tables (16-byte records first).
+struct TileTables {
+    size_t el4, txc, txp, bl, base_n, len_n, rxph, base_w, len_w, stages, act_n, act_w, act_g, act_c, total;
+};
+
+// Per-channel tables hold NG * CG records and per-wave tables NC * KW records: the
+// channels / waves past N / W are padding with zero weight, so a stage never needs
+// bounds checks.
+__host__ __device__ __forceinline__ TileTables tile_tables(int64_t N, int64_t W, int64_t NG, int64_t NC, int CG,
+                                                           int KW) {
+    TileTables t;
+    const size_t NP = (size_t)(NG * CG), WP = (size_t)(NC * KW);
+    (void)N;
+    (void)W;
+    size_t o = 0;
+    t.el4 = o;    o += 16 * NP;        // float4 per channel: x, y, z, window base
+    t.txc = o;    o += 16 * WP;        // float4 per wave: delay coefficients
+    t.txp = o;    o += 16 * WP;        // float4 per wave: phase offset, apodization, fs/c, kind
+    t.bl = o;     o += 8 * (NP + WP);  // int2 {window base, length}: channels, then waves
+    t.base_n = o; o += 4 * NP;
+    t.len_n = o;  o += 4 * NP;
+    t.rxph = o;   o += 4 * NP;         // phase (cycles) of each channel's window base
+    t.base_w = o; o += 4 * WP;
+    t.len_w = o;  o += 4 * WP;
+    t.stages = o; o += 4 * (size_t)(NG * NC);  // (outer << 16) | inner, loop order
+    t.act_n = o;  o += NP;
+    t.act_w = o;  o += WP;
+    t.act_g = o;  o += (size_t)NG;                       // channel groups
+    t.act_c = o;  o += (size_t)NC;                       // wave chunks
+    t.total = (o + 15) & ~size_t(15);
+    return t;
 }
 
 // Once per CTA, before its first tile: zero the stage buffers, so that units with
@@ -356,39 +394,56 @@ __device__ __forceinline__ void zero_slots() {
     __syncthreads();
 }
 
-// Beamform one tile of one frame (the whole CTA participates).
-__host__ __device__ __forceinline__ size_t tile_hdr_bytes(int64_t N, int64_t W, int64_t NG, int64_t NC) {
-    return 8 * (size_t)(N + W) + 4 * (size_t)(NG * NC) + (size_t)(N + W) + (size_t)(NG + NC);
-}
+__device__ __forceinline__ float frac_cycles(double v) { return (float)(v - floor(v)); }
 
-template <int MODE, bool CPLX, bool EPI>
+// Beamform one tile of one frame (the whole CTA participates).
+//
+// Delays are kept relative to integer window bases of the tile: for pixel p,
+//   s_tx(p, w) = (tau_tx - t0) fs - base_w,   s_rx(p, n) = tau_rx fs - base_n,
+// both in [0, kHalf], and the unit's sample position in slot (n, w) is
+// s_tx + s_rx.  The phase factors exp(i 2 pi fd tau) are formed from these
+// relative delays and a per-tile offset of each base (computed in double):
+//   fd tau_tx = (fd/fs) s_tx + frac(fd (base_w/fs + t0)),  fd tau_rx = (fd/fs) s_rx + frac(fd base_n / fs).
+// A plane or photoacoustic wave's s_tx is affine in the pixel position and a
+// spherical wave's is sigma |p - src| fs/c + const; the per-tile coefficients
+// sit in shared memory (txc, txp).
+template <int MODE, bool CPLX, bool EPI, int SHAPE>
 __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, int half = -1) {
-    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
-    constexpr int CG = StageShape<ORDER_A>::CG;
-    constexpr int KW = StageShape<ORDER_A>::KW;
-    constexpr int NS = StageShape<ORDER_A>::NS;
+    constexpr bool ORDER_A = Shape<SHAPE>::WAVES_OUTER;
+    constexpr int CG = Shape<SHAPE>::CG;
+    constexpr int KW = Shape<SHAPE>::KW;
+    constexpr int NS = CG * KW;
     static_assert(NS == kStageSlots, "stage buffers hold kStageSlots slots");
+    static_assert(MODE != USTB_DIM_RECEIVE || ORDER_A, "dimension.receive keeps waves outer");
+    static_assert((MODE != USTB_DIM_TRANSMIT && MODE != USTB_DIM_NONE) || !ORDER_A,
+                  "dimension.transmit / none keep channels outer");
     using Entry = typename EntryT<CPLX>::type;
     constexpr int ES = (int)sizeof(Entry);
 
-    const int64_t L = A.L, N = A.N, W = A.W, P = A.P;
+    const int64_t N = A.N, W = A.W, P = A.P;
     extern __shared__ __align__(16) unsigned char smem[];
     Entry* slots = reinterpret_cast<Entry*>(smem);
     const int NG = (int)((N + CG - 1) / CG), NC = (int)((W + KW - 1) / KW);
-    float* base_n = reinterpret_cast<float*>(smem + slot_buffer_bytes<CPLX>());  // integer-valued
-    int* len_n = reinterpret_cast<int*>(base_n + N);
-    float* base_w = reinterpret_cast<float*>(len_n + N);
-    int* len_w = reinterpret_cast<int*>(base_w + W);
-    int* stage_list = len_w + W;  // (outer index << 16) | inner index, loop order
-    unsigned char* act_n = reinterpret_cast<unsigned char*>(stage_list + NG * NC);
-    unsigned char* act_w = act_n + N;
-    unsigned char* act_g = act_w + W;  // channel groups
-    unsigned char* act_c = act_g + NG; // wave chunks
-    int2* bl_n = reinterpret_cast<int2*>(smem + slot_buffer_bytes<CPLX>() + ((tile_hdr_bytes(N, W, NG, NC) + 15) & ~size_t(15)));
-    int2* bl_w = bl_n + NG * CG;  // {window base, length} per channel / wave; length < 0: no copy
-    float4* el4 = reinterpret_cast<float4*>(bl_w + NC * KW);  // per channel: x, y, z, window base
+    const TileTables tt = tile_tables(N, W, NG, NC, CG, KW);
+    unsigned char* tb = smem + slot_buffer_bytes<CPLX>();
+    float4* el4 = reinterpret_cast<float4*>(tb + tt.el4);
+    float4* txc = reinterpret_cast<float4*>(tb + tt.txc);
+    float4* txp = reinterpret_cast<float4*>(tb + tt.txp);
+    int2* bl_n = reinterpret_cast<int2*>(tb + tt.bl);
+    int2* bl_w = bl_n + NG * CG;
+    float* base_n = reinterpret_cast<float*>(tb + tt.base_n);
+    int* len_n = reinterpret_cast<int*>(tb + tt.len_n);
+    float* rxph = reinterpret_cast<float*>(tb + tt.rxph);
+    float* base_w = reinterpret_cast<float*>(tb + tt.base_w);
+    int* len_w = reinterpret_cast<int*>(tb + tt.len_w);
+    int* stage_list = reinterpret_cast<int*>(tb + tt.stages);
+    unsigned char* act_n = tb + tt.act_n;
+    unsigned char* act_w = tb + tt.act_w;
+    unsigned char* act_g = tb + tt.act_g;
+    unsigned char* act_c = tb + tt.act_c;
     __shared__ float2 s_red[kTile / 32];
     __shared__ int s_nstages;
+    __shared__ int s_tx_general;  // a spherical or tabulated wave, or tabulated tx apodization
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -411,7 +466,24 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         box.lo[2] = r.x; box.hi[2] = r.y;
     }
 
-    // ---- per-tile window bases, lengths and activity ----------------------
+    // ---- per-tile window bases, lengths, activity and delay/phase coefficients ----
+    const double fd_fs = (double)A.fd / (double)A.fs;
+    if (tid == 0) s_tx_general = A.tx_apo_tab != nullptr || A.tx_delay_tab != nullptr;
+    for (int n = (int)N + tid; n < NG * CG; n += kTile) {  // padding channels: never active
+        el4[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+        base_n[n] = 0.f;
+        len_n[n] = 0;
+        rxph[n] = 0.f;
+        act_n[n] = 0;
+    }
+    for (int w = (int)W + tid; w < NC * KW; w += kTile) {  // padding waves: zero weight
+        txc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
+        txp[w] = make_float4(0.f, 0.f, 0.f, (float)USTB_WAVE_ZERO);
+        base_w[w] = 0.f;
+        len_w[w] = 0;
+        act_w[w] = 0;
+    }
+    __syncthreads();  // s_tx_general is set before the wave loop may raise it
     for (int64_t n = tid; n < N; n += kTile) {
         const float ex = __ldg(A.el + 3 * n), ey = __ldg(A.el + 3 * n + 1), ez = __ldg(A.el + 3 * n + 2);
         float dmin, dmax;
@@ -425,10 +497,11 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         el4[n] = make_float4(ex, ey, ez, base_n[n]);
         len_n[n] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
         act_n[n] = act ? 1 : 0;
+        rxph[n] = frac_cycles(fd_fs * (double)base_n[n]);
     }
     for (int64_t w = tid; w < W; w += kTile) {
         const ustb_wave wv = A.waves[w];
-        if (wv.kind == USTB_WAVE_TABLE) continue;
+        if (wv.kind == USTB_WAVE_TABLE) continue;  // bases from the table below
         float lo, hi;
         tx_tau_range(wv, box, lo, hi);
         lo = (lo - A.t0) * A.fs;
@@ -437,23 +510,58 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         const bool ok = (hi - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
         const bool act = A.tx_apo_tab != nullptr || wv.apodization != 0.f;
         if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-        base_w[w] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        if (wv.kind == USTB_WAVE_SPHERICAL && act) s_tx_general = 1;
+        const float bw = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+        base_w[w] = bw;
         len_w[w] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
         act_w[w] = act ? 1 : 0;
+        // s_tx(p) = (tau(p) - t0) fs - base_w; constant part in double
+        const double fs_c = (double)A.fs / (double)wv.sound_speed;
+        const double c0 = -((double)wv.delay + (double)A.t0) * (double)A.fs - (double)bw;
+        if (wv.kind == USTB_WAVE_PLANE)
+            txc[w] = make_float4((float)(wv.dir[0] * fs_c), (float)(wv.dir[1] * fs_c), (float)(wv.dir[2] * fs_c),
+                                 (float)c0);
+        else if (wv.kind == USTB_WAVE_SPHERICAL)
+            txc[w] = make_float4(wv.src[0], wv.src[1], wv.src[2], (float)(c0 + (double)wv.offset * fs_c));
+        else
+            txc[w] = make_float4(0.f, 0.f, 0.f, (float)c0);
+        txp[w] = make_float4(frac_cycles(fd_fs * ((double)bw + (double)A.t0 * (double)A.fs)), wv.apodization,
+                             (float)fs_c, (float)wv.kind);
     }
     if (A.tx_delay_tab) {  // tabulated transmit delays: the tile's actual range
         for (int64_t w = 0; w < W; ++w) {
-            if (A.waves[w].kind != USTB_WAVE_TABLE) continue;
+            const ustb_wave wv = A.waves[w];
+            if (wv.kind != USTB_WAVE_TABLE) continue;
             const float s = (__ldg(A.tx_delay_tab + w * P + p) - A.t0) * A.fs;
             const float2 r = block_minmax(live ? s : 3.4e38f, live ? s : -3.4e38f, s_red);
             if (tid == 0) {
                 const float base = floorf(r.x) - 1.f;
                 const bool ok = (r.y - base <= kHalf - 2.f) && fabsf(base) < 1.0e9f;
                 if (!ok) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
-                base_w[w] = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                const float bw = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+                base_w[w] = bw;
                 len_w[w] = (int)fminf(fmaxf(ceilf(r.y - base), 0.f), kHalf);
                 act_w[w] = 1;
+                txc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
+                txp[w] = make_float4(frac_cycles(fd_fs * ((double)bw + (double)A.t0 * (double)A.fs)),
+                                     wv.apodization, 0.f, (float)USTB_WAVE_TABLE);
             }
+        }
+    } else {
+        for (int64_t w = tid; w < W; w += kTile) {  // table waves without a table: tau = -delay
+            const ustb_wave wv = A.waves[w];
+            if (wv.kind != USTB_WAVE_TABLE) continue;
+            const float lo = (-wv.delay - A.t0) * A.fs;
+            const float base = floorf(lo) - 1.f;
+            const bool act = A.tx_apo_tab != nullptr || wv.apodization != 0.f;
+            const float bw = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
+            base_w[w] = bw;
+            len_w[w] = (int)fminf(fmaxf(ceilf(lo - base), 0.f), kHalf);
+            act_w[w] = act ? 1 : 0;
+            const double c0 = -((double)wv.delay + (double)A.t0) * (double)A.fs - (double)bw;
+            txc[w] = make_float4(0.f, 0.f, 0.f, (float)c0);
+            txp[w] = make_float4(frac_cycles(fd_fs * ((double)bw + (double)A.t0 * (double)A.fs)), wv.apodization,
+                                 0.f, (float)USTB_WAVE_ZERO);
         }
     }
     __syncthreads();
@@ -493,9 +601,9 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     const int nstages = s_nstages;
 
     const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
-    const float fd_c = A.fd * A.inv_c;
+    const float fdfs = (float)fd_fs;
     const int64_t frame_tr = f * W * N;  // first trace of this frame
-    const int Lc = (int)L;               // entries per trace
+    const int Lc = (int)A.L;             // entries per trace
     const uint32_t slots_s = (uint32_t)__cvta_generic_to_shared(slots);
     unsigned bufoff = 0;                 // byte offset of the current stage's buffer
     auto stage_o = [&](int si) { return stage_list[si] >> 16; };
@@ -526,7 +634,9 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         const uint32_t dst = slots_s + (uint32_t)((buf * NS + sl) * kSlot * ES);
         const int hl = lane & 15;
         if (i0 >= 0 && i0 + len <= Lc) {
-            for (int j = hl; j < len; j += 16) cp_async<ES>(dst + (uint32_t)(j * ES), src + i0 + j);
+            const Entry* sp = src + i0 + hl;
+            const uint32_t dp = dst + (uint32_t)(hl * ES);
+            for (int j = 0; j < len - hl; j += 16) cp_async<ES>(dp + (uint32_t)(j * ES), sp + j);
         } else {
             for (int j = hl; j < len; j += 16) {
                 const int i = i0 + j;
@@ -571,31 +681,64 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
                 apo = A.rx_apo_tab ? __ldg(A.rx_apo_tab + (int64_t)n * P + p) : rx_apodization(A, ex, ey, ez, px, py, pz);
                 if (!live) apo = 0.f;
                 if (CPLX) {
-                    const float2 e = phasor_cycles(r * fd_c + A.lens * A.fd);
+                    const float2 e = phasor_cycles(fmaf(s, fdfs, rxph[n]));
                     bb = make_float2(apo * e.x, apo * e.y);
                 } else {
                     bb = make_float2(apo, 0.f);
                 }
             }
-            srx[c] = fminf(fmaxf(s, 0.f), kHalf);  // NaN -> kHalf: stays inside the slot
+            srx[c] = fminf(fmaxf(s, 0.f), kHalf);  // NaN -> 0: stays inside the slot
             B[c] = bb;
             rxapo[c] = apo;
         }
     };
+    // Plane and photoacoustic waves (every tile without spherical or tabulated waves
+    // and without a tx apodization table): s_tx is affine in the pixel position and
+    // the weight is the wave's constant apodization times the phasor; padding and
+    // inactive waves carry apodization 0.  No branches.
+    const bool tx_affine = !s_tx_general;
+    auto setup_tx_affine = [&](int w0) {
+#pragma unroll
+        for (int k = 0; k < KW; ++k) {
+            const float4 cw = txc[w0 + k];
+            const float2 q = *reinterpret_cast<const float2*>(&txp[w0 + k]);
+            const float s = fmaf(cw.x, px, fmaf(cw.y, py, fmaf(cw.z, pz, cw.w)));
+            stx[k] = fminf(fmaxf(s, 0.f), kHalf);
+            if (CPLX) {
+                const float2 e = phasor_cycles(fmaf(s, fdfs, q.x));
+                Aw[k] = make_float2(q.y * e.x, q.y * e.y);
+            } else {
+                Aw[k] = make_float2(q.y, 0.f);
+            }
+        }
+    };
     auto setup_tx = [&](int w0) {
+        if (tx_affine) {
+            setup_tx_affine(w0);
+            return;
+        }
 #pragma unroll
         for (int k = 0; k < KW; ++k) {
             const int w = w0 + k;
-            float s = 0.f, apo = 0.f;
+            float s = 0.f;
             float2 a = make_float2(0.f, 0.f);
             if (w < W && act_w[w]) {
-                const ustb_wave wv = A.waves[w];
-                const float tau = tx_tau(A, wv, w, p, px, py, pz);
-                s = (tau - A.t0) * A.fs - base_w[w];
-                apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + (int64_t)w * P + p) : wv.apodization;
+                const float4 cw = txc[w];
+                const float4 q = txp[w];
+                const int kind = (int)q.w;
+                if (kind == USTB_WAVE_SPHERICAL) {
+                    const float dx = px - cw.x, dy = py - cw.y, dz = pz - cw.z;
+                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    s = fmaf(pz < cw.z ? -d : d, q.z, cw.w);
+                } else if (kind == USTB_WAVE_TABLE) {
+                    s = (__ldg(A.tx_delay_tab + w * P + p) - A.t0) * A.fs - base_w[w];
+                } else {  // plane; photoacoustic (zero coefficients)
+                    s = fmaf(cw.x, px, fmaf(cw.y, py, fmaf(cw.z, pz, cw.w)));
+                }
+                float apo = A.tx_apo_tab ? __ldg(A.tx_apo_tab + (int64_t)w * P + p) : q.y;
                 if (!live) apo = 0.f;
                 if (CPLX) {
-                    const float2 e = phasor_cycles(tau * A.fd);
+                    const float2 e = phasor_cycles(fmaf(s, fdfs, q.x));
                     a = make_float2(apo * e.x, apo * e.y);
                 } else {
                     a = make_float2(apo, 0.f);
@@ -647,6 +790,20 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         bufoff = (unsigned)(((si - s_lo) & 1) * NS * kSlot * ES);
     };
     const float2 zero2 = make_float2(0.f, 0.f);
+    // dimension.both: the pixel's sum, plain store or (split tiles) one of two partial sums
+    auto store_both = [&]() {
+        const float2 y = CPLX ? cmul(Y, ph) : Y;
+        if (half < 0) {
+            store_cube(p + A.f_f * f, y);
+        } else if (live && A.cube) {  // two partial sums per pixel: fl(a + b) in either order
+            if constexpr (CPLX) {
+                atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].x, y.x);
+                atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].y, y.y);
+            } else {
+                atomicAdd(&reinterpret_cast<float*>(A.cube)[p + A.f_f * f], y.x);
+            }
+        }
+    };
 
     if constexpr (ORDER_A) {
         int cur = -1;  // current wave chunk
@@ -710,19 +867,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         }
         if (cur >= 0) finish_chunk();
         zero_chunks(cur + 1, NC);
-        if (MODE == USTB_DIM_BOTH) {
-            const float2 y = CPLX ? cmul(Y, ph) : Y;
-            if (half < 0) {
-                store_cube(p + A.f_f * f, y);
-            } else if (live && A.cube) {  // two partial sums per pixel: fl(a + b) in either order
-                if constexpr (CPLX) {
-                    atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].x, y.x);
-                    atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].y, y.y);
-                } else {
-                    atomicAdd(&reinterpret_cast<float*>(A.cube)[p + A.f_f * f], y.x);
-                }
-            }
-        }
+        if (MODE == USTB_DIM_BOTH) store_both();
     } else {
         if (MODE == USTB_DIM_NONE) {  // units outside the active stages are zero
             for (int n = 0; n < N; ++n)
@@ -734,43 +879,39 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
                 for (int n = from * CG; n < min(to * CG, (int)N); ++n) store_cube(p + A.rx_f * n + A.f_f * f, zero2);
         };
         auto finish_group = [&]() {
-            if constexpr (MODE != USTB_DIM_TRANSMIT) return;
+            if constexpr (MODE == USTB_DIM_NONE) return;
             const int n0 = cur * CG;
             const int cg = min(CG, (int)N - n0);
 #pragma unroll
             for (int c = 0; c < CG; ++c) {
                 if (c >= cg) continue;
                 float2 y;
-                if constexpr (CPLX) y = cmul(cmul(B[c], make_float2(accr[c], acci[c])), ph);
+                if constexpr (CPLX) y = cmul(B[c], make_float2(accr[c], acci[c]));
                 else y = make_float2(B[c].x * accr[c], 0.f);
-                store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, y);
-                if constexpr (EPI) {
-                    eS.x += y.x;
-                    eS.y += y.y;
-                    eI += y.x * y.x + y.y * y.y;
-                    eM += rxapo[c] > A.cf_thr ? 1.f : 0.f;
-                    const float re = y.x;
-                    eR += msign(re) * sqrtf(fabsf(re));
-                    eQ += fabsf(re);
+                if constexpr (MODE == USTB_DIM_BOTH) {
+                    Y.x += y.x;
+                    Y.y += y.y;
+                } else {
+                    if constexpr (CPLX) y = cmul(y, ph);
+                    store_cube(p + A.rx_f * (n0 + c) + A.f_f * f, y);
+                    if constexpr (EPI) {
+                        eS.x += y.x;
+                        eS.y += y.y;
+                        eI += y.x * y.x + y.y * y.y;
+                        eM += rxapo[c] > A.cf_thr ? 1.f : 0.f;
+                        const float re = y.x;
+                        eR += msign(re) * sqrtf(fabsf(re));
+                        eQ += fabsf(re);
+                    }
                 }
             }
         };
-        for (int si = 0; si < nstages; ++si) {
-            const int og = stage_o(si);
-            if (og != cur) {
-                if (cur >= 0) finish_group();
-                zero_groups(cur + 1, og);
-                cur = og;
-                setup_rx(og * CG);
-#pragma unroll
-                for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
-            }
-            const int w0 = stage_w0(si), n0 = og * CG;
-            setup_tx(w0);
-            begin_stage(si);
+        unsigned gmask = 0;  // channels of the current group with a nonzero weight in this warp
+        constexpr unsigned kAll = (1u << CG) - 1u;
+        auto units = [&](int n0, int w0, auto all) {
 #pragma unroll
             for (int c = 0; c < CG; ++c) {
-                if (MODE != USTB_DIM_NONE && !__any_sync(0xffffffffu, B[c].x != 0.f || B[c].y != 0.f)) continue;
+                if (!decltype(all)::value && !((gmask >> c) & 1u)) continue;
 #pragma unroll
                 for (int k = 0; k < KW; ++k) {
                     const float2 v = interp(c, k, stx[k] + srx[c]);
@@ -788,9 +929,30 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
                     }
                 }
             }
+        };
+        for (int si = s_lo; si < s_hi; ++si) {
+            const int code = stage_list[si];
+            const int og = code >> 16, w0 = (code & 0xFFFF) * KW, n0 = og * CG;
+            if (og != cur) {
+                if (cur >= 0) finish_group();
+                zero_groups(cur + 1, og);
+                cur = og;
+                setup_rx(n0);
+                gmask = 0;
+#pragma unroll
+                for (int c = 0; c < CG; ++c)
+                    if (MODE == USTB_DIM_NONE || __any_sync(0xffffffffu, B[c].x != 0.f || B[c].y != 0.f)) gmask |= 1u << c;
+#pragma unroll
+                for (int c = 0; c < CG; ++c) accr[c] = acci[c] = 0.f;
+            }
+            setup_tx(w0);
+            begin_stage(si);
+            if (gmask == kAll) units(n0, w0, std::true_type{});
+            else units(n0, w0, std::false_type{});
         }
         if (cur >= 0) finish_group();
         zero_groups(cur + 1, NG);
+        if constexpr (MODE == USTB_DIM_BOTH) store_both();
         if constexpr (EPI) {
             if (live) {
                 const int64_t o = p + P * f;
@@ -806,14 +968,14 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     __syncthreads();  // the buffers and per-tile tables are reused by the next tile
 }
 
-// One launch per request: grid = (tiles, frames).
-template <int MODE, bool CPLX, bool EPI>
+// One launch per request: grid = (tiles x CTAs per tile, frames).
+template <int MODE, bool CPLX, bool EPI, int SHAPE>
 __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX>::value)) das_fast_kernel(const Params A) {
     zero_slots<CPLX>();
     if (MODE == USTB_DIM_BOTH && A.split == 2)
-        das_tile<MODE, CPLX, EPI>(A, (int)(blockIdx.x >> 1), (int64_t)blockIdx.y, (int)(blockIdx.x & 1));
+        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)(blockIdx.x >> 1), (int64_t)blockIdx.y, (int)(blockIdx.x & 1));
     else
-        das_tile<MODE, CPLX, EPI>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
+        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
 }
 
 // Persistent form: one CTA per SM pulls (request, frame, tile) work items from a
@@ -827,7 +989,7 @@ struct BatchParams {
     unsigned long long* counter;        // queue head (device scratch, zeroed per launch)
 };
 
-template <int MODE, bool CPLX, bool EPI>
+template <int MODE, bool CPLX, bool EPI, int SHAPE>
 __global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_constant__ BatchParams B) {
     __shared__ long long s_item;
     zero_slots<CPLX>();
@@ -842,29 +1004,39 @@ __global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_con
         while (r + 1 < B.n && B.first_item[r + 1] <= item) ++r;
         const Params& A = B.req[r];
         const int64_t local = item - B.first_item[r];
-        das_tile<MODE, CPLX, EPI>(A, (int)(local % A.n_tiles), local / A.n_tiles);
+        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)(local % A.n_tiles), local / A.n_tiles);
     }
 }
 
-template <int MODE, bool CPLX, bool EPI>
+template <bool CPLX, int SHAPE>
 size_t smem_bytes(int64_t N, int64_t W) {
-    constexpr bool ORDER_A = (MODE == USTB_DIM_BOTH || MODE == USTB_DIM_RECEIVE);
-    constexpr int CG = StageShape<ORDER_A>::CG, KW = StageShape<ORDER_A>::KW;
-    const size_t NG = (size_t)((N + CG - 1) / CG), NC = (size_t)((W + KW - 1) / KW);
-    const size_t hdr = tile_hdr_bytes(N, W, NG, NC);
-    return slot_buffer_bytes<CPLX>() + ((hdr + 15) & ~size_t(15)) + 8 * (NG * CG + NC * KW) + 16 * ((N + 1) & ~int64_t(1)) + 16;
+    constexpr int CG = Shape<SHAPE>::CG, KW = Shape<SHAPE>::KW;
+    const int64_t NG = (N + CG - 1) / CG, NC = (W + KW - 1) / KW;
+    return slot_buffer_bytes<CPLX>() + tile_tables(N, W, NG, NC, CG, KW).total;
 }
 
-template <int MODE, bool CPLX, bool EPI>
+// The stage shape a request runs with: ustb_das_geometry.stage_shape when given
+// (1: waves outer 2 x 16, 2: channels outer 8 x 4, 3: channels outer 16 x 2),
+// else the library's choice.  Returns the Shape<> index.
+int shape_for(int dim, int32_t requested) {
+    if (requested > 0) return requested - 1;
+    switch (dim) {
+        case USTB_DIM_RECEIVE: return 0;
+        case USTB_DIM_BOTH: return kBothShape;
+        default: return 1;
+    }
+}
+
+template <int MODE, bool CPLX, bool EPI, int SHAPE>
 int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
-    const size_t smem = smem_bytes<MODE, CPLX, EPI>(A.N, A.W);
+    const size_t smem = smem_bytes<CPLX, SHAPE>(A.N, A.W);
     int dev = 0, optin = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE,
                  "%lld channels / %lld waves need %zu bytes of shared memory per tile (limit %d)",
                  (long long)A.N, (long long)A.W, smem, optin);
-    auto kern = das_fast_kernel<MODE, CPLX, EPI>;
+    auto kern = das_fast_kernel<MODE, CPLX, EPI, SHAPE>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // dimension.both with few tiles (under 4 per SM): two CTAs per tile, each over half of
     // its stages, add their partial sums into the zeroed image, so the last wave of
@@ -882,7 +1054,7 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
     return USTB_OK;
 }
 
-template <int MODE, bool CPLX, bool EPI>
+template <int MODE, bool CPLX, bool EPI, int SHAPE>
 int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long long* counter, cudaStream_t s) {
     BatchParams B;
     B.n = n;
@@ -892,7 +1064,7 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     for (int i = 0; i < n; ++i) {
         B.req[i] = reqs[i];
         B.first_item[i + 1] = B.first_item[i] + reqs[i].n_tiles * frames[i];
-        smem = std::max(smem, smem_bytes<MODE, CPLX, EPI>(reqs[i].N, reqs[i].W));
+        smem = std::max(smem, smem_bytes<CPLX, SHAPE>(reqs[i].N, reqs[i].W));
     }
     if (B.first_item[n] == 0) return USTB_OK;
     int dev = 0, optin = 0, sms = 0;
@@ -901,7 +1073,7 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "a request needs %zu bytes of shared memory per tile (limit %d)",
                  smem, optin);
-    auto kern = das_fast_persistent<MODE, CPLX, EPI>;
+    auto kern = das_fast_persistent<MODE, CPLX, EPI, SHAPE>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     USTB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
     const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], (int64_t)sms);
@@ -910,31 +1082,32 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     return USTB_OK;
 }
 
-template <bool CPLX>
-int dispatch_batch(int dim, int epi, const Params* reqs, const int64_t* frames, int n,
-                   unsigned long long* counter, cudaStream_t s) {
+// Kernel variant of (dimension, epilogue, stage shape) for one request kind.
+template <bool CPLX, bool BATCH>
+int dispatch(int dim, int epi, int shape, const Params* reqs, const int64_t* frames, int n,
+             unsigned long long* counter, int64_t nt, int64_t F, cudaStream_t s) {
+#define USTB_RUN(M, E, S)                                                                      \
+    return BATCH ? launch_batch<M, CPLX, E, S>(reqs, frames, n, counter, s)                   \
+                 : launch<M, CPLX, E, S>(reqs[0], nt, F, s)
     switch (dim) {
-        case USTB_DIM_NONE: return launch_batch<USTB_DIM_NONE, CPLX, false>(reqs, frames, n, counter, s);
-        case USTB_DIM_RECEIVE: return launch_batch<USTB_DIM_RECEIVE, CPLX, false>(reqs, frames, n, counter, s);
+        case USTB_DIM_NONE:
+            if (shape == 2) USTB_RUN(USTB_DIM_NONE, false, 2);
+            USTB_RUN(USTB_DIM_NONE, false, 1);
+        case USTB_DIM_RECEIVE: USTB_RUN(USTB_DIM_RECEIVE, false, 0);
         case USTB_DIM_TRANSMIT:
             if constexpr (CPLX)
-                if (epi) return launch_batch<USTB_DIM_TRANSMIT, CPLX, true>(reqs, frames, n, counter, s);
-            return launch_batch<USTB_DIM_TRANSMIT, CPLX, false>(reqs, frames, n, counter, s);
-        default: return launch_batch<USTB_DIM_BOTH, CPLX, false>(reqs, frames, n, counter, s);
+                if (epi) {
+                    if (shape == 2) USTB_RUN(USTB_DIM_TRANSMIT, true, 2);
+                    USTB_RUN(USTB_DIM_TRANSMIT, true, 1);
+                }
+            if (shape == 2) USTB_RUN(USTB_DIM_TRANSMIT, false, 2);
+            USTB_RUN(USTB_DIM_TRANSMIT, false, 1);
+        default:
+            if (shape == 0) USTB_RUN(USTB_DIM_BOTH, false, 0);
+            if (shape == 2) USTB_RUN(USTB_DIM_BOTH, false, 2);
+            USTB_RUN(USTB_DIM_BOTH, false, 1);
     }
-}
-
-template <bool CPLX>
-int dispatch_mode(int dim, int epi, const Params& A, int64_t nt, int64_t F, cudaStream_t s) {
-    switch (dim) {
-        case USTB_DIM_NONE: return launch<USTB_DIM_NONE, CPLX, false>(A, nt, F, s);
-        case USTB_DIM_RECEIVE: return launch<USTB_DIM_RECEIVE, CPLX, false>(A, nt, F, s);
-        case USTB_DIM_TRANSMIT:
-            if constexpr (CPLX)
-                if (epi) return launch<USTB_DIM_TRANSMIT, CPLX, true>(A, nt, F, s);
-            return launch<USTB_DIM_TRANSMIT, CPLX, false>(A, nt, F, s);
-        default: return launch<USTB_DIM_BOTH, CPLX, false>(A, nt, F, s);
-    }
+#undef USTB_RUN
 }
 
 // ---- entries scratch ---------------------------------------------------------
@@ -1091,6 +1264,12 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
     A.flags = flags;
     USTB_REQUIRE(g->ctas_per_tile >= 0 && g->ctas_per_tile <= 2, USTB_E_ARG, "ctas_per_tile must be 0, 1 or 2");
     A.split = g->ctas_per_tile;  // 0: chosen at launch
+    USTB_REQUIRE(g->stage_shape >= 0 && g->stage_shape <= 3, USTB_E_ARG, "stage_shape must be 0, 1, 2 or 3");
+    USTB_REQUIRE(g->stage_shape == 0 || dimension == USTB_DIM_BOTH ||
+                     (dimension == USTB_DIM_RECEIVE) == (g->stage_shape == 1),
+                 USTB_E_ARG, "stage_shape %d does not fit dimension %d (receive: 1; transmit/none: 2 or 3)",
+                 (int)g->stage_shape, (int)dimension);
+    A.shape = shape_for(dimension, g->stage_shape);
     return USTB_OK;
 }
 
@@ -1110,8 +1289,8 @@ extern "C" int ustb_das_fast(const void* ch, int32_t storage, int32_t is_complex
     if (rc) return rc;
     A.entries = ent;
     const int64_t nt = g->n_tiles;
-    rc = is_complex ? dispatch_mode<true>(dimension, epilogue, A, nt, F, s)
-                    : dispatch_mode<false>(dimension, 0, A, nt, F, s);
+    rc = is_complex ? dispatch<true, false>(dimension, epilogue, A.shape, &A, nullptr, 1, nullptr, nt, F, s)
+                    : dispatch<false, false>(dimension, 0, A.shape, &A, nullptr, 1, nullptr, nt, F, s);
     const cudaError_t fe = cudaFreeAsync(ent, s);
     if (rc) return rc;
     USTB_CUDA(fe);
@@ -1151,8 +1330,8 @@ extern "C" int ustb_das_fast_entries(const void* entries, int32_t is_complex, in
     USTB_REQUIRE(((uintptr_t)entries & 15) == 0, USTB_E_ARG, "entries must be 16-byte aligned");
     A.entries = entries;
     const int64_t nt = g->n_tiles;
-    return is_complex ? dispatch_mode<true>(dimension, epilogue, A, nt, F, s)
-                      : dispatch_mode<false>(dimension, 0, A, nt, F, s);
+    return is_complex ? dispatch<true, false>(dimension, epilogue, A.shape, &A, nullptr, 1, nullptr, nt, F, s)
+                      : dispatch<false, false>(dimension, 0, A.shape, &A, nullptr, 1, nullptr, nt, F, s);
 }
 
 static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
@@ -1180,7 +1359,7 @@ static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t
             return rc;
         }
         frames[i] = q.F;
-        if (!empty) key[i] = (q.dimension * 2 + q.is_complex) * 2 + (q.epilogue ? 1 : 0);
+        if (!empty) key[i] = ((q.dimension * 2 + q.is_complex) * 2 + (q.epilogue ? 1 : 0)) * 4 + P[i].shape;
     }
     // every request's entry array: carved from the caller's workspace, or allocated
     // from the library pool and freed (stream-ordered) after the launches
@@ -1238,8 +1417,10 @@ static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t
                 return USTB_E_ARG;
             }
             const int rc = q.is_complex
-                               ? dispatch_batch<true>(q.dimension, q.epilogue, gp.data() + off, gf.data() + off, cnt, counter, s)
-                               : dispatch_batch<false>(q.dimension, 0, gp.data() + off, gf.data() + off, cnt, counter, s);
+                               ? dispatch<true, true>(q.dimension, q.epilogue, P[i].shape, gp.data() + off, gf.data() + off,
+                                                      cnt, counter, 0, 0, s)
+                               : dispatch<false, true>(q.dimension, 0, P[i].shape, gp.data() + off, gf.data() + off, cnt,
+                                                       counter, 0, 0, s);
             if (rc) {
                 release();
                 return rc;

@@ -204,9 +204,10 @@ class DAS:
         return ch
 
     def fast_geometry(self, dev, tile_block=None, tile_order: str = "cost",
-                      ctas_per_tile: int = 0) -> "fast.FastGeometry":
+                      ctas_per_tile: int = 0, stage_shape: int = 0) -> "fast.FastGeometry":
         """Device geometry for the fast engine; ``tile_block`` / ``tile_order`` /
-        ``ctas_per_tile`` as chosen by ``autotune`` (default: the library's own)."""
+        ``ctas_per_tile`` / ``stage_shape`` as chosen by ``autotune`` (default: the
+        library's own)."""
         from . import fast
 
         cd = self.channel_data
@@ -217,7 +218,8 @@ class DAS:
                                  self.receive_apodization, self.transmit_apodization,
                                  self.lens_delay, self.spherical_transmit_delay_model,
                                  self.pw_margin, self.blending_power, pixel_phase=ph,
-                                 tile_block=tile_block, tile_order=tile_order, ctas_per_tile=ctas_per_tile)
+                                 tile_block=tile_block, tile_order=tile_order, ctas_per_tile=ctas_per_tile,
+                                 stage_shape=stage_shape)
 
     def _go_fast(self) -> BeamformedData:
         from . import fast

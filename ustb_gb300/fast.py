@@ -49,7 +49,8 @@ class CGeometry(ctypes.Structure):
                 ("rx_window", ctypes.c_int32), ("rx_f_number", ctypes.c_float * 2),
                 ("rx_min_aperture", ctypes.c_float * 2), ("rx_max_aperture", ctypes.c_float * 2),
                 ("rx_use_origin", ctypes.c_int32), ("rx_origin", ctypes.c_float * 3),
-                ("cf_threshold", ctypes.c_float), ("ctas_per_tile", ctypes.c_int32)]
+                ("cf_threshold", ctypes.c_float), ("ctas_per_tile", ctypes.c_int32),
+                ("stage_shape", ctypes.c_int32)]
 
 
 class COutputs(ctypes.Structure):
@@ -255,7 +256,7 @@ class FastGeometry:
                  model: STDM = STDM.hybrid, pw_margin: float = 1e-3, blending_power: float = 0.5,
                  pixel_phase: Optional[np.ndarray] = None, cf_threshold: float = 0.16,
                  tiles: Optional[np.ndarray] = None, tile_block: Optional[Sequence[int]] = None,
-                 tile_order: str = "cost", ctas_per_tile: int = 0):
+                 tile_order: str = "cost", ctas_per_tile: int = 0, stage_shape: int = 0):
         dev = torch.device(device)
         rx = rx_apodization or Apodization()
         tx = tx_apodization or Apodization()
@@ -352,6 +353,10 @@ class FastGeometry:
             raise ValueError("ctas_per_tile must be 0 (library's choice), 1 or 2")
         g.ctas_per_tile = int(ctas_per_tile)
         self.ctas_per_tile = int(ctas_per_tile)
+        if stage_shape not in (0, 1, 2, 3):
+            raise ValueError("stage_shape must be 0 (library's choice), 1, 2 or 3")
+        g.stage_shape = int(stage_shape)
+        self.stage_shape = int(stage_shape)
         self.c = g
         self.device = dev
 
