@@ -43,6 +43,7 @@ namespace {
 
 constexpr int kTile = USTB_TILE_PIXELS;
 constexpr int kSlot = 160;                      // entries per (channel, wave) window
+constexpr int kRing = 2;                        // stage buffers: stage s + kRing - 1 is copied during stage s
 constexpr float kHalf = (float)(kSlot / 2 - 1);  // max relative delay of each component
 constexpr float kMagic = 8388608.0f;            // 2^23: floor via round-toward-zero add
 constexpr int kMagicBits = 0x4B000000;
@@ -285,6 +286,9 @@ __device__ __forceinline__ void cp_async(uint32_t dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+// all but the newest N commit groups of this thread have landed
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Conservative test that channel `n`'s receive window is zero over the whole tile
 // box: every window is 0 for ratio > 1/2 (apodization.m:172-186), and the ratio
@@ -343,16 +347,16 @@ struct Shape<2> {
 };
 constexpr int kStageSlots = 32;
 
-// Shared memory of one CTA: two stage buffers of kStageSlots slots x kSlot entries,
+// Shared memory of one CTA: kRing stage buffers of kStageSlots slots x kSlot entries,
 // then the per-tile tables (their size depends on N, W and the stage shape).
 template <bool CPLX>
 constexpr size_t slot_buffer_bytes() {
-    return (size_t)2 * kStageSlots * kSlot * (CPLX ? 16 : 8);
+    return (size_t)kRing * kStageSlots * kSlot * (CPLX ? 16 : 8);
 }
 
 // Byte offsets of the per-tile tables (16-byte records first).
 struct TileTables {
-    size_t el4, txc, txp, bl, base_n, len_n, rxph, base_w, len_w, stages, act_n, act_w, act_g, act_c, total;
+    size_t el4, txc, txp, bl, base_n, len_n, rxph, base_w, len_w, stages, olist, act_n, act_w, act_g, act_c, total;
 };
 
 // Per-channel tables hold NG * CG records and per-wave tables NC * KW records: the
@@ -375,6 +379,7 @@ __host__ __device__ __forceinline__ TileTables tile_tables(int64_t N, int64_t W,
     t.base_w = o; o += 4 * WP;
     t.len_w = o;  o += 4 * WP;
     t.stages = o; o += 4 * (size_t)(NG * NC);  // (outer << 16) | inner, loop order
+    t.olist = o;  o += 4 * (size_t)(NG + NC);  // active outer indices, then active inner indices
     t.act_n = o;  o += NP;
     t.act_w = o;  o += WP;
     t.act_g = o;  o += (size_t)NG;                       // channel groups
@@ -586,16 +591,43 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         act_c[k] = a;
     }
     __syncthreads();
-    if (tid == 0) {
-        int cnt = 0;
+    // stage list: every (active outer, active inner) pair in loop order.  Warp 0
+    // compacts the active outer and inner indices (ballots), then all threads fill in
+    // the pairs.
+    __shared__ int s_nout, s_nin;
+    {
         const int NO = ORDER_A ? NC : NG, NI = ORDER_A ? NG : NC;
         const unsigned char* ao = ORDER_A ? act_c : act_g;
         const unsigned char* ai = ORDER_A ? act_g : act_c;
-        for (int o = 0; o < NO; ++o)
-            if (ao[o])
-                for (int i = 0; i < NI; ++i)
-                    if (ai[i]) stage_list[cnt++] = (o << 16) | i;
-        s_nstages = cnt;
+        int* olist = reinterpret_cast<int*>(tb + tt.olist);
+        int* ilist = olist + NO;
+        if (warp == 0) {
+            int cnt = 0;
+            for (int b = 0; b < NO; b += 32) {
+                const bool a = b + lane < NO && ao[b + lane];
+                const unsigned m = __ballot_sync(0xffffffffu, a);
+                if (a) olist[cnt + __popc(m & ((1u << lane) - 1u))] = b + lane;
+                cnt += __popc(m);
+            }
+            int cin = 0;
+            for (int b = 0; b < NI; b += 32) {
+                const bool a = b + lane < NI && ai[b + lane];
+                const unsigned m = __ballot_sync(0xffffffffu, a);
+                if (a) ilist[cin + __popc(m & ((1u << lane) - 1u))] = b + lane;
+                cin += __popc(m);
+            }
+            if (lane == 0) {
+                s_nout = cnt;
+                s_nin = cin;
+                s_nstages = cnt * cin;
+            }
+        }
+        __syncthreads();
+        const int no = s_nout, ni = s_nin;
+        for (int t = tid; t < no * ni; t += kTile) {
+            const int r = t / ni, q = t - r * ni;
+            stage_list[t] = (olist[r] << 16) | ilist[q];
+        }
     }
     __syncthreads();
     const int nstages = s_nstages;
@@ -782,12 +814,23 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     // its partial sum to the (zeroed) output; -1: the whole list, plain stores
     const int s_lo = (half == 1) ? nstages / 2 : 0;
     const int s_hi = (half == 0) ? nstages / 2 : nstages;
-    if (s_lo < s_hi) issue(s_lo, 0);
+    // A ring of kRing stage buffers: the copies of the first kRing - 1 stages are
+    // issued up front, then stage si waits for its own copies (older commit groups),
+    // one barrier publishes them and frees stage si - 1's buffer, which takes stage
+    // si + kRing - 1's copies.  Stages past the end commit empty groups, so that every
+    // thread's count of outstanding groups stays kRing - 1.
+#pragma unroll
+    for (int d = 0; d < kRing - 1; ++d) {
+        if (s_lo + d < s_hi) issue(s_lo + d, d);
+        else cp_async_commit();
+    }
     auto begin_stage = [&](int si) {
-        cp_async_wait_all();
+        cp_async_wait_group<kRing - 2>();
         __syncthreads();
-        if (si + 1 < s_hi) issue(si + 1, (si + 1 - s_lo) & 1);
-        bufoff = (unsigned)(((si - s_lo) & 1) * NS * kSlot * ES);
+        const int nx = si + kRing - 1;
+        if (nx < s_hi) issue(nx, (nx - s_lo) % kRing);
+        else cp_async_commit();
+        bufoff = (unsigned)(((si - s_lo) % kRing) * NS * kSlot * ES);
     };
     const float2 zero2 = make_float2(0.f, 0.f);
     // dimension.both: the pixel's sum, plain store or (split tiles) one of two partial sums
@@ -965,7 +1008,8 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
             }
         }
     }
-    __syncthreads();  // the buffers and per-tile tables are reused by the next tile
+    cp_async_wait_all();  // only empty groups remain
+    __syncthreads();      // the buffers and per-tile tables are reused by the next tile
 }
 
 // One launch per request: grid = (tiles x CTAs per tile, frames).
