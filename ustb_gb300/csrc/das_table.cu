@@ -67,23 +67,71 @@ __device__ __forceinline__ void store(const TableArgs& A, int64_t idx, int64_t f
 // those units).  All WC sample loads are then in flight together.
 constexpr int WC = 8;
 
-template <bool CPLX, int FC, bool PER_WAVE, int NACC>
-__device__ __forceinline__ void chunk_units(const TableArgs& A, int64_t n, int64_t w0, int wc, int64_t f0,
+// A table value that is read once per wave chunk: kept out of L1 so that it does not
+// evict the channel-data lines the sample gathers reuse.
+__device__ __forceinline__ float ld_stream(const float* p) {
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];\n" : "=f"(v) : "l"(p));
+    return v;
+}
+
+// das_c's n0 = (int)s and floor(s) (das_c.cpp:381-383).  For traces of at most 2^23
+// samples the integer part comes from adding 2^23 with round-toward-zero: it equals
+// (int)s for 0 <= s < 2^23, and negative, too large, NaN or infinite s give indices
+// outside (0, L - 1), so those units stay invalid as in das_c; for the valid units
+// (s >= 1) floor(s) = (int)s and the fraction s - floor(s) is the same float.
+// Longer traces use the conversion instructions.
+template <bool MAGIC>
+__device__ __forceinline__ int trunc_floor(float s, float& fl) {
+    if constexpr (MAGIC) {
+        const float t = __fadd_rz(s, 8388608.0f);
+        fl = __fsub_rn(t, 8388608.0f);
+        return __float_as_int(t) - 0x4B000000;
+    } else {
+        fl = floorf(s);
+        return __float2int_rz(s);
+    }
+}
+
+// Prefetch into L1 the sample lines of one channel's WC units, so that their loads a
+// channel later hit L1 instead of waiting on L2 (same index arithmetic as chunk_units).
+template <bool CPLX, typename IDX, bool MAGIC>
+__device__ __forceinline__ void prefetch_units(const TableArgs& A, IDX nL, const IDX* wbase, int wc, const float* txd,
+                                               float rxd, float rxa) {
+    if (rxa == 0.0f) return;
+    const int Lm1 = (int)(A.L - 1);
+#pragma unroll
+    for (int k = 0; k < WC; ++k) {
+        const float denay = __fmul_rn(__fsub_rn(__fadd_rn(txd[k], rxd), A.t0), A.fs);
+        float fl;
+        const int n0 = trunc_floor<MAGIC>(denay, fl);
+        if (k < wc && n0 > 0 && n0 < Lm1) {
+            const char* x = reinterpret_cast<const char*>(A.ch) + (size_t)(nL + wbase[k] + (IDX)n0) * (CPLX ? 8 : 4);
+            asm volatile("prefetch.global.L1 [%0];\n" ::"l"(x));
+        }
+    }
+}
+
+// IDX: int32_t when every sample index of the call fits 31 bits, else int64_t.
+template <bool CPLX, int FC, bool PER_WAVE, int NACC, typename IDX, bool MAGIC>
+__device__ __forceinline__ void chunk_units(const TableArgs& A, IDX nL, const IDX* wbase, int wc, int64_t f0,
                                             int nf, const float* txd, const float* txa, float rxd, float rxa,
                                             Acc<CPLX, FC>* acc) {
     float a[WC], b[WC], wr[WC], wi[WC];
-    int64_t base[WC];
+    IDX base[WC];
     bool ok[WC];
+    const int Lm1 = (int)(A.L - 1);
 #pragma unroll
     for (int k = 0; k < WC; ++k) {
         const float delay = __fadd_rn(txd[k], rxd);
         const float apo = __fmul_rn(txa[k], rxa);
         const float denay = __fmul_rn(__fsub_rn(delay, A.t0), A.fs);
-        const int n0 = __float2int_rz(denay);
-        ok[k] = k < wc && txa[k] != 0.0f && rxa != 0.0f && n0 > 0 && (int64_t)n0 < A.L - 1;
-        b[k] = __fsub_rn(denay, floorf(denay));
+        float fl;
+        const int n0 = trunc_floor<MAGIC>(denay, fl);
+        ok[k] = k < wc && txa[k] != 0.0f && rxa != 0.0f && n0 > 0 && n0 < Lm1;
+        b[k] = __fsub_rn(denay, fl);
         a[k] = __fsub_rn(1.0f, b[k]);
-        base[k] = A.L * n + A.LN * (w0 + (k < wc ? k : 0)) + (ok[k] ? n0 : 1) + f0 * A.LNW;
+        base[k] = nL + wbase[k] + (IDX)(ok[k] ? n0 : 1);
         if (CPLX) {
             float c, s;
             ustb::expi_reduced(__fmul_rn(A.wd, delay), c, s);
@@ -119,7 +167,7 @@ __device__ __forceinline__ void chunk_units(const TableArgs& A, int64_t n, int64
     }
 }
 
-template <int MODE, bool CPLX, int FC>
+template <int MODE, bool CPLX, int FC, typename IDX, bool MAGIC>
 __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) {
     const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     if (p >= A.P) return;
@@ -142,14 +190,38 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
             for (int64_t w0 = 0; w0 < A.W; w0 += WC) {
                 const int wc = (int)min((int64_t)WC, A.W - w0);
                 load_tx(w0, wc);
+                IDX wbase[WC];
+#pragma unroll
+                for (int k = 0; k < WC; ++k) wbase[k] = (IDX)(A.LN * (w0 + (k < wc ? k : 0)) + f0 * A.LNW);
                 if (MODE == USTB_DIM_RECEIVE)
 #pragma unroll
                     for (int k = 0; k < WC; ++k) acc[k].zero();
-                for (int64_t n = 0; n < A.N; ++n) {
-                    const float rxa = __ldg(A.apo_rx + P * n + p);
+                // receive values are loaded two channels ahead and the next channel's
+                // sample lines prefetched into L1 while this channel is computed
+                const float* pa = A.apo_rx + p;
+                const float* pd = A.d_rx + p;
+                float rxa1 = ld_stream(pa), rxd1 = ld_stream(pd), rxa2 = 0.f, rxd2 = 0.f;
+                if (A.N > 1) {
+                    rxa2 = ld_stream(pa + P);
+                    rxd2 = ld_stream(pd + P);
+                }
+                pa += 2 * P;
+                pd += 2 * P;
+                if (FC == 1) prefetch_units<CPLX, IDX, MAGIC>(A, (IDX)0, wbase, wc, txd, rxd1, rxa1);
+                IDX nL = 0;
+                for (int64_t n = 0; n < A.N; ++n, nL += (IDX)A.L) {
+                    const float rxa = rxa1, rxd = rxd1;
+                    rxa1 = rxa2;
+                    rxd1 = rxd2;
+                    if (n + 2 < A.N) {
+                        rxa2 = ld_stream(pa);
+                        rxd2 = ld_stream(pd);
+                        pa += P;
+                        pd += P;
+                    }
+                    if (FC == 1 && n + 1 < A.N) prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
                     if (rxa == 0.0f) continue;
-                    const float rxd = __ldg(A.d_rx + P * n + p);
-                    chunk_units<CPLX, FC, PER_WAVE, NACC>(A, n, w0, wc, f0, nf, txd, txa, rxd, rxa, acc);
+                    chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, nL, wbase, wc, f0, nf, txd, txa, rxd, rxa, acc);
                 }
                 if (MODE == USTB_DIM_RECEIVE)
 #pragma unroll
@@ -165,11 +237,15 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
                 for (int64_t w0 = 0; w0 < A.W; w0 += WC) {
                     const int wc = (int)min((int64_t)WC, A.W - w0);
                     load_tx(w0, wc);
+                    IDX wbase[WC];
+#pragma unroll
+                    for (int k = 0; k < WC; ++k) wbase[k] = (IDX)(A.LN * (w0 + (k < wc ? k : 0)) + f0 * A.LNW);
                     if (MODE == USTB_DIM_NONE)
 #pragma unroll
                         for (int k = 0; k < WC; ++k) acc[k].zero();
                     if (rxa != 0.0f)
-                        chunk_units<CPLX, FC, PER_WAVE, NACC>(A, n, w0, wc, f0, nf, txd, txa, rxd, rxa, acc);
+                        chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, (IDX)(A.L * n), wbase, wc, f0, nf, txd, txa, rxd,
+                                                                   rxa, acc);
                     if (MODE == USTB_DIM_NONE)
 #pragma unroll
                         for (int k = 0; k < WC; ++k)
@@ -181,15 +257,28 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
     }
 }
 
-template <int MODE, bool CPLX>
-void launch_fc(const TableArgs& A, cudaStream_t s) {
+template <int MODE, bool CPLX, typename IDX, bool MAGIC>
+void launch_idx(const TableArgs& A, cudaStream_t s) {
     const unsigned grid = (unsigned)((A.P + kThreads - 1) / kThreads);
     if (A.F == 1)
-        das_table_kernel<MODE, CPLX, 1><<<grid, kThreads, 0, s>>>(A);
+        das_table_kernel<MODE, CPLX, 1, IDX, MAGIC><<<grid, kThreads, 0, s>>>(A);
     else if (A.F == 2)
-        das_table_kernel<MODE, CPLX, 2><<<grid, kThreads, 0, s>>>(A);
+        das_table_kernel<MODE, CPLX, 2, IDX, MAGIC><<<grid, kThreads, 0, s>>>(A);
     else
-        das_table_kernel<MODE, CPLX, 4><<<grid, kThreads, 0, s>>>(A);
+        das_table_kernel<MODE, CPLX, 4, IDX, MAGIC><<<grid, kThreads, 0, s>>>(A);
+}
+
+// 32-bit sample indices when every index of the call (and one past it) fits 31 bits;
+// the float trick of trunc_floor for traces of at most 2^23 samples
+template <int MODE, bool CPLX>
+void launch_fc(const TableArgs& A, cudaStream_t s) {
+    const bool short_traces = A.L <= ((int64_t)1 << 23);
+    if (A.LNW * A.F < (int64_t)INT32_MAX - 1 && short_traces)
+        launch_idx<MODE, CPLX, int32_t, true>(A, s);
+    else if (short_traces)
+        launch_idx<MODE, CPLX, int64_t, true>(A, s);
+    else
+        launch_idx<MODE, CPLX, int64_t, false>(A, s);
 }
 
 template <bool CPLX>

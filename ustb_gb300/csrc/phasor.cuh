@@ -17,8 +17,11 @@ constexpr float kInvTwoPi = (float)(1.0 / kTwoPiD);
 // (two FMAs), then the hardware sine/cosine approximations on the reduced
 // argument (absolute error below 4e-7 on [-pi, pi]).  x itself is used exactly
 // as given, so callers that round x like the reference does reproduce its phase.
+// The nearest integer to x / 2pi is taken by adding and subtracting 1.5 * 2^23
+// (exact for |x / 2pi| < 2^22; any integer k keeps the reduction exact), which
+// keeps the conversion pipe free for the sine and cosine.
 __device__ __forceinline__ void expi_reduced(float x, float& c, float& s) {
-    const float k = rintf(x * kInvTwoPi);
+    const float k = __fsub_rn(__fmaf_rn(x, kInvTwoPi, 12582912.0f), 12582912.0f);
     float r = fmaf(-k, kTwoPiHi, x);
     r = fmaf(-k, kTwoPiLo, r);
     __sincosf(r, &s, &c);
