@@ -315,6 +315,23 @@ def serving_mix(device, n_requests, seed, torch):
         torch.cuda.synchronize()
     plain_s = time.perf_counter() - t
 
+    # the same requests on the fast path (FP16 storage), one launch per request and one
+    # request at a time: what continuous batching is measured against
+    def run_fast(k):
+        wl, das, ch, st, cplx = prep[k]
+        epi = wl.epilogue is not None
+        fast.das_fast(st, Precision.fp16, cplx, srv.plans[k], wl.dimension, L=ch.shape[-1], epilogue=epi,
+                      cube=not epi, check=False)
+
+    for k in kinds:
+        run_fast(k)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for k in order:
+        run_fast(k)
+        torch.cuda.synchronize()
+    serial_fast_s = time.perf_counter() - t
+
     def make(i, order=order):
         k = order[i]
         wl, das, ch, st, cplx = prep[k]
@@ -332,7 +349,17 @@ def serving_mix(device, n_requests, seed, torch):
     rate = 0.7 * n_requests / sat["seconds"]
     srv.completed.clear()
     jobs = srv.run(list(serving.poisson_arrivals(n_requests, rate, seed)), make)
-    stats = serving.latency_stats(jobs)
+    stats = serving.latency_stats(jobs, per_key=True)
+    # the same arrivals with a sixth of the SMs kept from the large requests for the small ones
+    lsrv = serving.Server(device, hbm_budget_bytes=150e9, max_batch=32,
+                          reserve_sms=torch.cuda.get_device_properties(device).multi_processor_count // 6)
+    for k in kinds:
+        lsrv.add_plan(k, srv.plans[k])
+    lsrv.run([0.0] * 8, make)
+    lsrv.completed.clear()
+    lburst = serving.latency_stats(lsrv.run([0.0] * n_requests, make))
+    lsrv.completed.clear()
+    lstats = serving.latency_stats(lsrv.run(list(serving.poisson_arrivals(n_requests, rate, seed)), make), per_key=True)
     # the same burst through the library's own server (ustb_serve_*: resident plans,
     # scheduler and completion threads in C++)
     from ustb_gb300 import plan as native
@@ -375,13 +402,24 @@ def serving_mix(device, n_requests, seed, torch):
         "served_frames_per_s": round(sat["frames_per_s"], 1),
         "plain_fp32_frames_per_s": round(n_requests / plain_s, 1),
         "speedup_vs_plain": round(sat["frames_per_s"] / (n_requests / plain_s), 2),
+        "serial_fast_frames_per_s": round(n_requests / serial_fast_s, 1),
+        "speedup_vs_serial_fast": round(sat["frames_per_s"] / (n_requests / serial_fast_s), 3),
+        "policy": f"small requests batched per kernel variant (<= 32 per launch, {srv.max_inflight} streams); "
+                  f"requests above {srv.large_units:.0e} units alone on another stream, queued back to back, "
+                  f"with all {srv.large_ctas} SMs",
+        "latency_policy": {"reserve_sms": lsrv.reserve_sms, "large_ctas": lsrv.large_ctas,
+                           "served_frames_per_s": round(lburst["frames_per_s"], 1),
+                           "latency_at_same_arrivals": {"p50_ms": round(lstats["p50_ms"], 3),
+                                                        "p99_ms": round(lstats["p99_ms"], 3),
+                                                        "per_kind": lstats["per_kind"]}},
         "launches_for_stream": launches,
         "native_server": {"frames_per_s": round(n_requests / native_s, 1),
                           "speedup_vs_plain": round(plain_s / native_s, 2), "flags": int(nflags),
                           "api": "ustb_plan_create + ustb_serve_submit/wait (C++ scheduler and completion "
                                  "threads, persistent batches within a 16 GB entries budget)"},
         "latency_at_70pct_load": {"arrival_rate_hz": round(rate, 1), "p50_ms": round(stats["p50_ms"], 3),
-                                  "p99_ms": round(stats["p99_ms"], 3), "frames_per_s": round(stats["frames_per_s"], 1)},
+                                  "p99_ms": round(stats["p99_ms"], 3), "frames_per_s": round(stats["frames_per_s"], 1),
+                                  "per_kind": stats["per_kind"]},
         "per_kind": per_kind,
         "hbm_budget_gb": 150, "storage": "fp16",
         "rel_l2_vs_fp64_oracle": {k: float(f"{v:.3g}") for k, v in errs.items()},

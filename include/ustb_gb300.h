@@ -310,6 +310,16 @@ int64_t ustb_das_fast_workspace_bytes(const ustb_das_request* reqs, int32_t n);
 int ustb_das_fast_batch_ws(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
                            int64_t workspace_bytes, void* stream);
 
+/*
+ * ustb_das_fast_batch / _ws with a bound on the persistent launch's CTAs:
+ * max_ctas > 0 runs at most that many CTAs (one per SM), leaving the other SMs to
+ * launches on other streams, e.g. small requests served while a large one runs;
+ * 0 = one CTA per SM.  workspace may be NULL (library pool, as
+ * ustb_das_fast_batch).  No reference counterpart (the reference serves nothing).
+ */
+int ustb_das_fast_batch_ex(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
+                           int64_t workspace_bytes, int32_t max_ctas, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Resident plans and the continuous-batching server                         */
 /* ------------------------------------------------------------------------ */

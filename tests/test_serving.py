@@ -46,7 +46,10 @@ def fake_server(monkeypatch):
         def __init__(self, *a, **k):
             self.outputs = {"cube": None}
 
-    def fake_batch(reqs, scratch=None, stream=None):
+    launched = []
+
+    def fake_batch(reqs, scratch=None, stream=None, max_ctas=0):
+        launched.append((len(reqs), max_ctas))
         return FakeTensor(8)
 
     def fake_event():
@@ -67,8 +70,9 @@ def fake_server(monkeypatch):
             return False
 
     monkeypatch.setattr(serving.torch.cuda, "stream", lambda s: Ctx())
-    srv = serving.Server("cpu", hbm_budget_bytes=10_000, max_batch=3, max_inflight=2)
+    srv = serving.Server("cpu", hbm_budget_bytes=10_000, max_batch=3, max_inflight=2, large_queue=2)
     srv.add_plan("a", FakeGeom())
+    srv.launched = launched
     return srv, events
 
 
@@ -127,6 +131,18 @@ def test_latency_stats():
     assert st["frames_per_s"] == pytest.approx(20 / 9.01)
 
 
+def test_one_launch_per_kernel_variant(fake_server):
+    srv, events = fake_server
+    srv.budget = 1e9
+    srv.max_inflight = 3
+    kinds = [3, 2, 3, 3, 2]  # dimension both / transmit interleaved
+    for d in kinds:
+        srv.submit(serving.Job("a", FakeTensor(100), 1, True, 1, 16, d))
+    srv.poll()
+    # the three dimension.both jobs share one launch, the two transmit jobs another
+    assert sorted(n for n, _ in srv.launched) == [2, 3] and not srv.pending
+
+
 def test_large_requests_launch_alone(fake_server):
     srv, events = fake_server
     srv.budget = 1e9
@@ -139,4 +155,37 @@ def test_large_requests_launch_alone(fake_server):
         srv.submit(serving.Job("s", FakeTensor(100), 1, True, 1, 16, 3))  # 80 units each
     srv.poll()
     # the large job went alone, the three small ones together in the second launch
-    assert srv.launches == 2 and not srv.pending
+    assert srv.launches == 2 and not srv.pending and not srv.pending_large
+    # the large launch runs with SMs - reserve CTAs (every SM by default)
+    assert srv.launched[0] == (1, srv.large_ctas) and srv.launched[1] == (3, 0)
+    assert srv.large_ctas == 152
+    lat = serving.Server("cpu", reserve_sms=25)
+    assert lat.large_ctas == 127
+
+
+def test_small_requests_flow_past_a_running_large_one(fake_server):
+    srv, events = fake_server
+    srv.budget = 1e9
+    srv.large_units = 500
+    small = FakeGeom()
+    small.P = 10
+    srv.add_plan("s", small)
+    srv.large_queue = 1
+    srv.submit(serving.Job("a", FakeTensor(100), 1, True, 1, 16, 3))  # large, in flight below
+    srv.submit(serving.Job("a", FakeTensor(100), 1, True, 1, 16, 3))  # a second large one waits
+    srv.poll()
+    assert len(srv.large_inflight) == 1 and len(srv.pending_large) == 1
+    # small requests arriving while the large launch runs are served without waiting for it
+    for _ in range(5):
+        srv.submit(serving.Job("s", FakeTensor(100), 1, True, 1, 16, 3))
+    srv.poll()
+    assert srv.launches == 3 and len(srv.pending) == 0  # 3 + 2 small jobs in two launches
+    events[1].done = events[2].done = True
+    assert srv.poll() == 5
+    assert len(srv.pending_large) == 1  # the first large one has not finished
+    events[0].done = True
+    assert srv.poll() == 1 and not srv.pending_large  # its successor starts at once
+    for e in events:
+        e.done = True
+    srv.drain()
+    assert len(srv.completed) == 7 and srv.used == 0

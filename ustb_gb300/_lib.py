@@ -37,6 +37,7 @@ SIGNATURES = {
     "ustb_das_fast_entries": (ctypes.c_int, [vp, i32, i64, i64, i64, i64, vp, i32, i32, vp, vp, vp]),
     "ustb_das_fast_workspace_bytes": (i64, [vp, i32]),
     "ustb_das_fast_batch_ws": (ctypes.c_int, [vp, i32, vp, vp, i64, vp]),
+    "ustb_das_fast_batch_ex": (ctypes.c_int, [vp, i32, vp, vp, i64, i32, vp]),
     "ustb_convert_channels": (ctypes.c_int, [vp, i32, vp, i32, i64, f32, vp]),
     "ustb_plan_create": (ctypes.c_int, [vp, vp]),
     "ustb_plan_destroy": (ctypes.c_int, [vp]),

@@ -1099,7 +1099,8 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
 }
 
 template <int MODE, bool CPLX, bool EPI, int SHAPE>
-int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long long* counter, cudaStream_t s) {
+int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long long* counter, int max_ctas,
+                 cudaStream_t s) {
     BatchParams B;
     B.n = n;
     B.counter = counter;
@@ -1120,7 +1121,9 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     auto kern = das_fast_persistent<MODE, CPLX, EPI, SHAPE>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     USTB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
-    const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], (int64_t)sms);
+    // one CTA per SM, or fewer (max_ctas) to leave SMs to launches on other streams
+    const int64_t ctas = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
+    const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], ctas);
     kern<<<grid, kTile, smem, s>>>(B);
     USTB_CUDA(cudaGetLastError());
     return USTB_OK;
@@ -1129,9 +1132,9 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
 // Kernel variant of (dimension, epilogue, stage shape) for one request kind.
 template <bool CPLX, bool BATCH>
 int dispatch(int dim, int epi, int shape, const Params* reqs, const int64_t* frames, int n,
-             unsigned long long* counter, int64_t nt, int64_t F, cudaStream_t s) {
+             unsigned long long* counter, int64_t nt, int64_t F, cudaStream_t s, int max_ctas = 0) {
 #define USTB_RUN(M, E, S)                                                                      \
-    return BATCH ? launch_batch<M, CPLX, E, S>(reqs, frames, n, counter, s)                   \
+    return BATCH ? launch_batch<M, CPLX, E, S>(reqs, frames, n, counter, max_ctas, s)         \
                  : launch<M, CPLX, E, S>(reqs[0], nt, F, s)
     switch (dim) {
         case USTB_DIM_NONE:
@@ -1379,9 +1382,10 @@ extern "C" int ustb_das_fast_entries(const void* entries, int32_t is_complex, in
 }
 
 static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
-                               int64_t workspace_bytes, void* stream) {
+                               int64_t workspace_bytes, int32_t max_ctas, void* stream) {
     ustb::clear_error();
     USTB_REQUIRE(n >= 0 && (n == 0 || reqs), USTB_E_ARG, "bad request array");
+    USTB_REQUIRE(max_ctas >= 0, USTB_E_ARG, "max_ctas must be >= 0 (0: one CTA per SM)");
     USTB_REQUIRE(scratch, USTB_E_ARG, "scratch pointer is NULL");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t* flags = reinterpret_cast<uint32_t*>(scratch);
@@ -1462,9 +1466,9 @@ static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t
             }
             const int rc = q.is_complex
                                ? dispatch<true, true>(q.dimension, q.epilogue, P[i].shape, gp.data() + off, gf.data() + off,
-                                                      cnt, counter, 0, 0, s)
+                                                      cnt, counter, 0, 0, s, max_ctas)
                                : dispatch<false, true>(q.dimension, 0, P[i].shape, gp.data() + off, gf.data() + off, cnt,
-                                                       counter, 0, 0, s);
+                                                       counter, 0, 0, s, max_ctas);
             if (rc) {
                 release();
                 return rc;
@@ -1476,7 +1480,12 @@ static int das_fast_batch_impl(const ustb_das_request* reqs, int32_t n, uint64_t
 }
 
 extern "C" int ustb_das_fast_batch(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* stream) {
-    return das_fast_batch_impl(reqs, n, scratch, nullptr, 0, stream);
+    return das_fast_batch_impl(reqs, n, scratch, nullptr, 0, 0, stream);
+}
+
+extern "C" int ustb_das_fast_batch_ex(const ustb_das_request* reqs, int32_t n, uint64_t* scratch, void* workspace,
+                                      int64_t workspace_bytes, int32_t max_ctas, void* stream) {
+    return das_fast_batch_impl(reqs, n, scratch, workspace, workspace_bytes, max_ctas, stream);
 }
 
 extern "C" int64_t ustb_das_fast_workspace_bytes(const ustb_das_request* reqs, int32_t n) {
@@ -1491,5 +1500,5 @@ extern "C" int ustb_das_fast_batch_ws(const ustb_das_request* reqs, int32_t n, u
         ustb::set_error("workspace pointer is NULL (ustb_das_fast_batch allocates its own)");
         return USTB_E_ARG;
     }
-    return das_fast_batch_impl(reqs, n, scratch, workspace, workspace_bytes, stream);
+    return das_fast_batch_impl(reqs, n, scratch, workspace, workspace_bytes, 0, stream);
 }

@@ -523,13 +523,15 @@ def workspace_bytes(requests: Sequence[Request]) -> int:
 
 
 def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] = None, stream=None,
-                   workspace: Optional[torch.Tensor] = None):
+                   workspace: Optional[torch.Tensor] = None, max_ctas: int = 0):
     """Beamform a batch of requests with the persistent work-queue kernel
-    (``ustb_das_fast_batch``).  Returns the int64 scratch tensor (word 0 = flags).
+    (``ustb_das_fast_batch_ex``).  Returns the int64 scratch tensor (word 0 = flags).
 
     ``workspace``: optional uint8 device tensor of at least ``workspace_bytes(requests)``
     bytes (256-byte aligned, as torch allocations are) that holds the interpolation
-    entries; without it the library allocates them from its own pool."""
+    entries; without it the library allocates them from its own pool.
+    ``max_ctas``: at most this many persistent CTAs (0 = one per SM), so that launches
+    on other streams can use the remaining SMs meanwhile."""
     if not requests:
         return scratch
     dev = requests[0].ch.device
@@ -540,10 +542,10 @@ def das_fast_batch(requests: Sequence[Request], scratch: Optional[torch.Tensor] 
     st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
     with torch.cuda.device(dev):
         if workspace is None:
-            _lib.call("ustb_das_fast_batch", ctypes.addressof(arr), n, scratch.data_ptr(), st)
+            _lib.call("ustb_das_fast_batch_ex", ctypes.addressof(arr), n, scratch.data_ptr(), None, 0, int(max_ctas), st)
         else:
-            _lib.call("ustb_das_fast_batch_ws", ctypes.addressof(arr), n, scratch.data_ptr(), workspace.data_ptr(),
-                      workspace.numel() * workspace.element_size(), st)
+            _lib.call("ustb_das_fast_batch_ex", ctypes.addressof(arr), n, scratch.data_ptr(), workspace.data_ptr(),
+                      workspace.numel() * workspace.element_size(), int(max_ctas), st)
     return scratch
 
 
