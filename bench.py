@@ -22,10 +22,11 @@ datasets.
            the CF/DMAS epilogue, synthetic transmit aperture, 3D matrix array),
            served with FP16 storage by continuous batching into persistent
            launches, against the same requests beamformed one at a time by the
-           plain FP32 das_c-exact kernel.
-``--impl reference`` times the reference's CPU implementation of the path
-           (the oracle port of das_c; the reference's own das_c build is
-           x86-only) on the host cores.
+           plain FP32 das_c-exact kernel and by the fast path.
+``--impl reference`` times the reference's CPU implementation of the path on
+           the host cores: its own das_c, compiled from the staged source on this
+           machine (the bit-identical oracle port where it was not built), and
+           beside it its own das_cuda on the GPU (``reference_gpu_das_cuda``).
 Multi-GPU runs are replicas: every rank beamforms its own frames.
 """
 from __future__ import annotations
@@ -164,18 +165,24 @@ def cuda_time(fn, steps, flush, stream, torch):
 
 # ---------------------------------------------------------------------------
 def cpu_reference(ch_np, fs, t0, fd, tabs, dim, target_s=12.0, steps=1):
-    """The das_c port on the host cores over a strided pixel sample."""
+    """The reference's own das_c (built from its source into oracle/_ref, on all host
+    cores through its std::thread parallel_for) over a strided pixel sample; the
+    bit-identical port where das_c was not built on this machine."""
     from oracle import oracle as O
 
     tx_apo, rx_apo, tx_delay, rx_delay = tabs
     P = tx_apo.shape[0]
     threads = os.cpu_count() or 1
+    use_ref = O.have_reference()
 
     def run(stride):
         sel = np.arange(0, P, stride)
         t = time.perf_counter()
-        O.das_f32(ch_np, fs, t0, tx_apo[sel], rx_apo[sel], tx_delay[sel], rx_delay[sel], fd, dim,
-                  threads=threads)
+        if use_ref:
+            O.das_c_ref(ch_np, fs, t0, tx_apo[sel], rx_apo[sel], tx_delay[sel], rx_delay[sel], fd, dim)
+        else:
+            O.das_f32(ch_np, fs, t0, tx_apo[sel], rx_apo[sel], tx_delay[sel], rx_delay[sel], fd, dim,
+                      threads=threads)
         return time.perf_counter() - t, sel.size
 
     dt, n = run(200)
@@ -186,9 +193,35 @@ def cpu_reference(ch_np, fs, t0, fd, tabs, dim, target_s=12.0, steps=1):
         times.append(dt)
     L, N, W, F = ch_np.shape
     t = statistics.median(times)
-    return {"value": n * N * W * F / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"every {stride}-th pixel ({n} of {P} pixels, all channels/waves), {t:.1f} s per pass, "
-                      f"oracle/das_port.c oracle_das_f32 (bit-identical to das_c) on {threads} threads"}
+    what = ("the reference's +mex/source/das_c.cpp compiled unmodified (oracle/_ref/libdas_c_ref.so), "
+            f"parallel_for over {threads} threads" if use_ref else
+            f"oracle/das_port.c oracle_das_f32 (bit-identical to das_c) on {threads} threads")
+    return {"value": n * N * W * F / t / 1e9, "unit": UNIT, "cores": threads,
+            "kind": "reference" if use_ref else "port",
+            "sample": f"every {stride}-th pixel ({n} of {P} pixels, all channels/waves), {t:.1f} s per pass, {what}"}
+
+
+def das_cuda_reference(ch_np, fs, t0, fd, tabs, steps=3):
+    """The reference's das_cuda (+mex/source/das_cuda.cu compiled unmodified for sm_103a)
+    on the whole frame, timed as its MEX call is used: host buffers in, host image out
+    (tables and channel data copied every call).  None where it was not built."""
+    from oracle import oracle as O
+
+    if not O.have_cuda_reference():
+        return None
+    tx_apo, rx_apo, tx_delay, rx_delay = tabs
+    O.das_cuda_ref(ch_np, fs, t0, tx_apo, rx_apo, tx_delay, rx_delay, fd)  # warm-up
+    times = []
+    for _ in range(max(1, steps)):
+        t = time.perf_counter()
+        out = O.das_cuda_ref(ch_np, fs, t0, tx_apo, rx_apo, tx_delay, rx_delay, fd)
+        times.append(time.perf_counter() - t)
+    L, N, W, F = ch_np.shape
+    P = tx_apo.shape[0]
+    ms = statistics.median(times) * 1e3
+    return {"ms_per_frame": round(ms, 3), "value": round(P * N * W * F / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
+            "call": "mex.das_cuda argument layout (das.m:262-271), host buffers, dimension both, median of "
+                    f"{len(times)} calls", "output": out}
 
 
 def fp64_subset_reference(wl, das, ch_matlab, sel):
@@ -947,6 +980,19 @@ def main_reference(args, rank, world):
                                   "400x400 pixels, dimension both", "units_per_step": units},
            "cpu_baseline": cb,
            "e2e": {"value": round(val, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if device.type == "cuda":
+        # the reference's own GPU point beside it: das_cuda on the same frame
+        dc = das_cuda_reference(ch_np, fs, t0, fd, tabs)
+        if dc is not None:
+            from oracle import oracle as O
+
+            out = dc.pop("output")
+            sel = np.arange(0, tabs[0].shape[0], 97)
+            ref = O.das_f32(ch_np, fs, t0, tabs[0][sel], tabs[1][sel], tabs[2][sel], tabs[3][sel], fd, 3)
+            dc["rel_l2_vs_das_c_port"] = float(f"{np.linalg.norm(out[sel] - ref) / np.linalg.norm(ref):.3g}")
+            res["reference_gpu_das_cuda"] = dc
+        else:
+            res["reference_gpu_das_cuda"] = {"unavailable": "das_cuda was not built on this machine"}
     print(json.dumps(res), flush=True)
 
 

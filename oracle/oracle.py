@@ -12,7 +12,12 @@ What is here:
 * ``das_c_ref``    — the reference's own das_c (+mex/source/das_c.cpp) compiled
                      unmodified by ``make -C oracle ref`` into oracle/_ref/.
                      Available only where the reference sources were present at
-                     build time; returns None otherwise.
+                     build time (the checkout, or the copy ``make -C oracle stage``
+                     puts into the git-ignored oracle/_ref/src/ so that it travels to
+                     the GPU machine); returns None otherwise.
+* ``das_cuda_ref`` — the reference's own das_cuda (+mex/source/das_cuda.cu,
+                     dimension both only) compiled unmodified for sm_103a by
+                     ``make -C oracle ref_cuda``; None where it was not built.
 * ``coherence_factor`` / ``sdmas_value`` — FP64 numpy restatements of
                      +postprocess/coherence_factor.m:100-135 and of the per-pixel
                      term of +postprocess/simplified_delay_multiply_and_sum.m:140-148.
@@ -58,9 +63,12 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _PORT_SO = os.path.join(_HERE, "_build", "liboracle.so")
 _REF_SO = os.path.join(_HERE, "_ref", "libdas_c_ref.so")
+_CUDA_SO = os.path.join(_HERE, "_ref", "libdas_cuda_ref.so")
+_STAGED = os.path.join(_HERE, "_ref", "src")
 
 _port = None
 _ref = None
+_cuda_ref = None
 
 _i64 = ctypes.c_int64
 _f32 = ctypes.c_float
@@ -69,14 +77,26 @@ _ptr = ctypes.c_void_p
 
 
 def build(reference: Optional[str] = None) -> None:
-    """Compile the C restatement, and the reference's own das_c from the checkout at
-    ``reference`` (or ``$USTB_REFERENCE_ROOT``) when one is given and holds its source."""
+    """Compile the C restatement; and the reference's own das_c and das_cuda, from the
+    checkout at ``reference`` (or ``$USTB_REFERENCE_ROOT``), whose two sources are then
+    also staged into oracle/_ref/src/, or else from an earlier staged copy."""
+    import shutil
     import subprocess
 
     subprocess.check_call(["make", "-s", "-C", _HERE, "all"])
     ref = reference or os.environ.get("USTB_REFERENCE_ROOT")
+    args = []
     if ref and os.path.isfile(os.path.join(ref, "+mex", "source", "das_c.cpp")):
-        subprocess.check_call(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"])
+        subprocess.check_call(["make", "-s", "-C", _HERE, "stage", f"REF={ref}"])
+    elif not os.path.isfile(os.path.join(_STAGED, "das_c.cpp")):
+        return
+    subprocess.check_call(["make", "-s", "-C", _HERE, "ref"] + args)
+    if shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc"):
+        env = dict(os.environ)
+        if not shutil.which("nvcc"):
+            env["NVCC"] = "/usr/local/cuda/bin/nvcc"
+        # the reference GPU point is optional: a failed build leaves it unavailable
+        subprocess.call(["make", "-s", "-C", _HERE, "ref_cuda"] + args, env=env)
 
 
 def _load_port():
@@ -112,6 +132,27 @@ def _load_ref():
 
 def have_reference() -> bool:
     return _load_ref() is not None
+
+
+def _load_cuda_ref():
+    global _cuda_ref
+    if _cuda_ref is None:
+        if not os.path.isfile(_CUDA_SO):
+            return None
+        try:
+            lib = ctypes.CDLL(_CUDA_SO)
+        except OSError:
+            return None
+        lib.das_cuda_ref_run.restype = ctypes.c_int
+        lib.das_cuda_ref_run.argtypes = [_ptr, _i64, _i64, _i64, _i64, _f32, _f32, _ptr, _ptr, _ptr,
+                                         _ptr, _i64, _f32, ctypes.c_int32, _ptr, ctypes.c_char_p,
+                                         ctypes.c_int, ctypes.c_int32]
+        _cuda_ref = lib
+    return _cuda_ref
+
+
+def have_cuda_reference() -> bool:
+    return _load_cuda_ref() is not None
 
 
 def _dims(ch):
@@ -180,6 +221,27 @@ def das_c_ref(ch, fs, t0, apo_tx, apo_rx, delay_tx, delay_rx, fd, dim) -> Option
     rc = lib.das_c_ref_run(c.ctypes.data, L, N, W, F, float(np.float32(fs)), float(np.float32(t0)),
                            atx.ctypes.data, arx.ctypes.data, dtx.ctypes.data, drx.ctypes.data, P,
                            float(np.float32(fd)), int(dim), out.ctypes.data, err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return out
+
+
+def das_cuda_ref(ch, fs, t0, apo_tx, apo_rx, delay_tx, delay_rx, fd, gpu=0) -> Optional[np.ndarray]:
+    """The reference's das_cuda itself on GPU ``gpu`` (dimension both; host buffers in
+    and out, as its MEX call takes them).  None when it was not built here."""
+    lib = _load_cuda_ref()
+    if lib is None:
+        return None
+    L, N, W, F = _dims(ch)
+    c = _f(ch, np.complex64).reshape((L, N, W, F), order="F")
+    atx, arx = _f(apo_tx, np.float32), _f(apo_rx, np.float32)
+    dtx, drx = _f(delay_tx, np.float32), _f(delay_rx, np.float32)
+    P = atx.shape[0]
+    out = np.zeros(out_shape(P, N, W, F, 3), dtype=np.complex64, order="F")
+    err = ctypes.create_string_buffer(512)
+    rc = lib.das_cuda_ref_run(c.ctypes.data, L, N, W, F, float(np.float32(fs)), float(np.float32(t0)),
+                              atx.ctypes.data, arx.ctypes.data, dtx.ctypes.data, drx.ctypes.data, P,
+                              float(np.float32(fd)), 3, out.ctypes.data, err, 512, int(gpu))
     if rc != 0:
         raise ValueError(err.value.decode())
     return out

@@ -1,2 +1,5 @@
-/* Stand-in for MATLAB's matrix.h: everything lives in the mex.h shim. Oracle only. */
+/*
+ * Stand-in for MATLAB's matrix.h: the mxArray API lives in the mex.h stand-in.
+ * TEST INFRASTRUCTURE ONLY (see mex.h).
+ */
 #include "mex.h"

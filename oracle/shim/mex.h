@@ -55,6 +55,7 @@ static inline size_t mxGetNumberOfElements(const mxArray* a) {
     for (mwSize d : a->dims) n *= d;
     return n;
 }
+static inline bool mxIsScalar(const mxArray* a) { return mxGetNumberOfElements(a) == 1; }
 static inline mxComplexSingle* mxGetComplexSingles(const mxArray* a) {
     /* MATLAB returns NULL for a real array; keep that behaviour. */
     if (a->cls != mxSINGLE_CLASS || !a->complex_) return nullptr;
