@@ -771,8 +771,8 @@ def profile_post(args, torch):
                ustb_demodulate_filtfilt);
     image:     the diverging-wave sector image (256 azimuths x 512 depths) -> 512 x 512
                log-compressed Cartesian image (ustb_scan_convert);
-    coherence: its 64-channel cube (dimension.transmit) -> phase and generalized
-               coherence factors;
+    coherence: its 64-channel cube (dimension.transmit) -> phase, generalized and
+               plain coherence factors over the channels;
     capon:     the same cube -> Capon minimum variance (32-element subarrays, +-1.5
                wavelengths of depth averaging, 1 % diagonal loading)."""
     from ustb_gb300 import fast, image, postprocess, preprocess, synth
@@ -826,7 +826,10 @@ def profile_post(args, torch):
             out.update(pixels=nz * nx, channels=int(cube.shape[2]), L_elements=32, K_samples=K)
         else:
             cube = o["cube"]
-            fn = lambda: (postprocess.phase_coherence_factor(cube), postprocess.generalized_coherence_factor(cube))
+            from ustb_gb300.enums import Dimension
+
+            fn = lambda: (postprocess.phase_coherence_factor(cube), postprocess.generalized_coherence_factor(cube),
+                          postprocess.coherence_factor(cube, Dimension.receive))
             out.update(cube_bytes=int(cube.numel() * 8))
     for _ in range(args.warmup):
         fn()

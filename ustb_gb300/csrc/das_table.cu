@@ -187,6 +187,18 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
         const int nf = (int)min((int64_t)FC, A.F - f0);
         if (MODE == USTB_DIM_RECEIVE || MODE == USTB_DIM_BOTH) {
             if (MODE == USTB_DIM_BOTH) acc[0].zero();
+            // the warp's channels with a nonzero receive weight lie in [nlo, nhi]: one scan
+            // of the apodization column, so that every wave chunk reads the receive tables
+            // of those channels only (the others are skipped per unit anyway)
+            int nlo = (int)A.N, nhi = -1;
+            for (int n = 0; n < (int)A.N; ++n)
+                if (ld_stream(A.apo_rx + P * n + p) != 0.0f) {
+                    nlo = min(nlo, n);
+                    nhi = n;
+                }
+            const unsigned live = __activemask();
+            nlo = __reduce_min_sync(live, nlo);
+            nhi = __reduce_max_sync(live, nhi);
             for (int64_t w0 = 0; w0 < A.W; w0 += WC) {
                 const int wc = (int)min((int64_t)WC, A.W - w0);
                 load_tx(w0, wc);
@@ -198,28 +210,33 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
                     for (int k = 0; k < WC; ++k) acc[k].zero();
                 // receive values are loaded two channels ahead and the next channel's
                 // sample lines prefetched into L1 while this channel is computed
-                const float* pa = A.apo_rx + p;
-                const float* pd = A.d_rx + p;
-                float rxa1 = ld_stream(pa), rxd1 = ld_stream(pd), rxa2 = 0.f, rxd2 = 0.f;
-                if (A.N > 1) {
+                // (no receive weight in this warp: nhi < nlo, the loop below runs no channel)
+                const float* pa = A.apo_rx + P * max(nlo, 0) + p;
+                const float* pd = A.d_rx + P * max(nlo, 0) + p;
+                float rxa1 = 0.f, rxd1 = 0.f, rxa2 = 0.f, rxd2 = 0.f;
+                if (nlo <= nhi) {
+                    rxa1 = ld_stream(pa);
+                    rxd1 = ld_stream(pd);
+                }
+                if (nlo + 1 <= nhi) {
                     rxa2 = ld_stream(pa + P);
                     rxd2 = ld_stream(pd + P);
                 }
                 pa += 2 * P;
                 pd += 2 * P;
-                if (FC == 1) prefetch_units<CPLX, IDX, MAGIC>(A, (IDX)0, wbase, wc, txd, rxd1, rxa1);
-                IDX nL = 0;
-                for (int64_t n = 0; n < A.N; ++n, nL += (IDX)A.L) {
+                IDX nL = (IDX)A.L * (IDX)nlo;
+                if (FC == 1 && nlo <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL, wbase, wc, txd, rxd1, rxa1);
+                for (int n = nlo; n <= nhi; ++n, nL += (IDX)A.L) {
                     const float rxa = rxa1, rxd = rxd1;
                     rxa1 = rxa2;
                     rxd1 = rxd2;
-                    if (n + 2 < A.N) {
+                    if (n + 2 <= nhi) {
                         rxa2 = ld_stream(pa);
                         rxd2 = ld_stream(pd);
                         pa += P;
                         pd += P;
                     }
-                    if (FC == 1 && n + 1 < A.N) prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
+                    if (FC == 1 && n + 1 <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
                     if (rxa == 0.0f) continue;
                     chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, nL, wbase, wc, f0, nf, txd, txa, rxd, rxa, acc);
                 }
