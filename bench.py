@@ -144,6 +144,20 @@ def make_headline(device):
     return wl, das, ch
 
 
+def tuned_geometry(das, wl, st, prec, cplx, L, device, F=1, epilogue=False):
+    """The request's FastGeometry with the tile plan and stage shape the autotuner picks
+    (cached per device and shape), timed on this request's own data."""
+    from ustb_gb300 import autotune, fast
+
+    dim = int(wl.dimension)
+    cd = wl.channel_data
+    run = lambda g: fast.das_fast(st, prec, cplx, g, dim, F=F, L=L, epilogue=epilogue, cube=not epilogue)
+    key = autotune.shape_key(wl.scan, cd.N_channels, cd.N_waves, L, F, prec, dim, cplx, device)
+    choice = autotune.tune(lambda b, o, c, sh: das.fast_geometry(device, b, o, c, sh), run,
+                           key + ("|epi" if epilogue else ""), scan=wl.scan, both=dim == 3, dimension=dim)
+    return das.fast_geometry(device, choice.block, choice.order, choice.ctas_per_tile, choice.stage_shape), choice
+
+
 def active_units(tx_apo, rx_apo, F=1):
     """Units with nonzero tx and rx apodization: the ones das_c evaluates."""
     ntx = (tx_apo != 0).sum(axis=1).astype(np.int64)
@@ -293,13 +307,17 @@ def serving_mix(device, n_requests, seed, torch):
     srv = serving.Server(device, hbm_budget_bytes=150e9, max_batch=32, max_inflight=2)
     prep = {}
     plain = {}
+    tuned = {}
     for k in kinds:
         wl = synth.CONFIGS[k](device=device)
         das = build_das(wl)
-        geom = das.fast_geometry(device)
         ch = channel_tensor(wl.channel_data.data, device)
         cplx = ch.is_complex()
         st = fast.convert_channels(ch, Precision.fp16)
+        geom, choice = tuned_geometry(das, wl, st, Precision.fp16, cplx, ch.shape[-1], device,
+                                      epilogue=wl.epilogue is not None)
+        tuned[k] = {"block": choice.block, "order": choice.order, "stage_shape": choice.stage_shape,
+                    "ctas_per_tile": choice.ctas_per_tile}
         srv.add_plan(k, geom)
         prep[k] = (wl, das, ch, st, cplx)
         # plain path: das_c-exact FP32 kernel on resident single-precision tables
@@ -456,6 +474,7 @@ def serving_mix(device, n_requests, seed, torch):
         "per_kind": per_kind,
         "hbm_budget_gb": 150, "storage": "fp16",
         "rel_l2_vs_fp64_oracle": {k: float(f"{v:.3g}") for k, v in errs.items()},
+        "tile_plans": tuned,
         "plain_path": "ustb_das_table_f32 (das_c-exact FP32 tables resident), one request at a time",
     }
 
@@ -482,9 +501,10 @@ def hfr_ensemble(device, torch, reps=5, plain_frames=20):
     sub = fast.convert_channels(x[:8].contiguous(), Precision.fp16, scale)
     run = lambda g: fast.das_fast(sub, Precision.fp16, True, g, int(wl.dimension), F=8, L=L)
     key = autotune.shape_key(wl.scan, N, W, L, 8, Precision.fp16, wl.dimension, True, device)
-    choice = autotune.tune(lambda b, o, c: das.fast_geometry(device, b, o, c), run, key, scan=wl.scan)
+    choice = autotune.tune(lambda b, o, c, sh: das.fast_geometry(device, b, o, c, sh), run, key, scan=wl.scan,
+                           dimension=int(wl.dimension))
     del sub
-    geom = das.fast_geometry(device, choice.block, choice.order)
+    geom = das.fast_geometry(device, choice.block, choice.order, 0, choice.stage_shape)
     ens = Ensemble(geom, F, L, wl.dimension, Precision.fp16, scale, graph=True)
     ens.run(x)
     torch.cuda.synchronize()
@@ -560,6 +580,7 @@ def hfr_ensemble(device, torch, reps=5, plain_frames=20):
         "launch": "one CUDA graph replay per ensemble: int16->FP16 conversion, entries pass, "
                   "one persistent launch over all (frame, tile) items",
         "tile_plan": {"block": list(choice.block) if choice.block else "planner default",
+                      "stage_shape": choice.stage_shape,
                       "order": choice.order, "tuned_ms_8_frames": round(choice.ms, 3)},
         "rel_l2_vs_fp64_oracle_frame0": float(f"{err:.3g}"),
         "storage": "fp16",
@@ -613,12 +634,13 @@ def main():
     act = active_units(tabs[0], tabs[1], F)
     fs, t0, fd = (float(np.float32(cd.sampling_frequency)), float(np.float32(cd.initial_time)),
                   float(np.float32(cd.modulation_frequency)))
-    geom = das.fast_geometry(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     flags = torch.zeros(1, dtype=torch.int32, device=dev)
     st32 = fast.convert_channels(ch, Precision.fp32)
     st16 = fast.convert_channels(ch, Precision.fp16)
+    # the tile plan and stage shape the autotuner picks for this shape (cached per device)
+    geom, plan = tuned_geometry(das, wl, st32, Precision.fp32, True, L, dev)
 
     def fast_step(st, prec):
         return lambda: fast.das_fast(st, prec, True, geom, 3, L=L, flags=flags, check=False)
@@ -726,6 +748,9 @@ def main():
                                          "rel_l2_vs_das_c_port": parity["table_vs_das_c_port"]},
             "parity": parity,
             "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
+            "tile_plan": {"block": list(plan.block) if plan.block else "planner default", "order": plan.order,
+                          "stage_shape": plan.stage_shape, "ctas_per_tile": plan.ctas_per_tile,
+                          "tuned_ms": round(plan.ms, 4)},
         },
         "roofline": {
             "bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_peak, 2), "unit": "TFLOP/s",

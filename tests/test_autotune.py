@@ -44,3 +44,43 @@ def test_cache_roundtrip_skips_the_search(tmp_path, monkeypatch):
     assert got.block == (16, 32, 1) and got.order == "scan" and got.ms == 1.5 and not calls
     data = json.load(open(tmp_path / "t.json"))
     assert data["k"]["order"] == "scan"
+
+
+def test_candidates_cover_the_stage_shapes_of_each_mode():
+    s2 = LinearScan(np.linspace(-1e-2, 1e-2, 256), np.linspace(5e-3, 5e-2, 512))
+    for dim, shapes in ((3, {1, 2, 3}), (1, {1}), (2, {2, 3}), (0, {2, 3})):
+        got = {c.stage_shape for c in autotune.candidates(s2, both=dim == 3, dimension=dim) if c.stage_shape}
+        assert got == shapes
+
+
+def test_tune_times_every_candidate_and_caches_the_stage_shape(tmp_path, monkeypatch):
+    monkeypatch.setenv("USTB_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
+    s2 = LinearScan(np.linspace(-1e-2, 1e-2, 64), np.linspace(5e-3, 5e-2, 64))
+    made = []
+
+    class Ev:
+        t = 0.0
+
+        def __init__(self, enable_timing=True):
+            pass
+
+        def record(self):
+            self.at = Ev.t
+
+        def elapsed_time(self, other):
+            return other.at - self.at
+
+    def make(block, order, cpt, shape):
+        made.append((block, order, cpt, shape))
+        return (block, order, cpt, shape)
+
+    def run(g):  # stage shape 3 is the fastest candidate
+        Ev.t += 1.0 if g[3] == 3 else 2.0
+
+    monkeypatch.setattr(autotune.torch.cuda, "Event", Ev)
+    monkeypatch.setattr(autotune.torch.cuda, "synchronize", lambda *a: None)
+    best = autotune.tune(make, run, "k3", scan=s2, both=True, dimension=3)
+    assert best.stage_shape == 3 and {m[3] for m in made} >= {1, 2, 3}
+    assert json.load(open(tmp_path / "t.json"))["k3"]["stage_shape"] == 3
+    again = autotune.tune(lambda *a: 1 / 0, run, "k3")  # from the cache, no search
+    assert again.stage_shape == 3

@@ -90,11 +90,13 @@ def test_autotuned_plan_gives_the_same_image(hfr, cuda_dev, tmp_path, monkeypatc
     st = fast.convert_channels(x, Precision.fp16, wl.info["scale"])
     run = lambda g: fast.das_fast(st, Precision.fp16, True, g, int(wl.dimension), F=F, L=L)
     key = autotune.shape_key(wl.scan, N, W, L, F, Precision.fp16, wl.dimension, True, cuda_dev)
-    choice = autotune.tune(lambda b, o, c: das.fast_geometry(cuda_dev, b, o, c), run, key, scan=wl.scan, both=True)
+    choice = autotune.tune(lambda b, o, c, sh: das.fast_geometry(cuda_dev, b, o, c, sh), run, key, scan=wl.scan,
+                           both=True, dimension=int(wl.dimension))
     assert choice.ms > 0
     again = autotune.tune(lambda *a: 1 / 0, run, key)  # served from the cache
     assert (again.block, again.order, again.ctas_per_tile) == (choice.block, choice.order, choice.ctas_per_tile)
-    tuned = run(das.fast_geometry(cuda_dev, choice.block, choice.order, choice.ctas_per_tile))["cube"]
+    tuned = run(das.fast_geometry(cuda_dev, choice.block, choice.order, choice.ctas_per_tile,
+                                  choice.stage_shape))["cube"]
     default = run(das.fast_geometry(cuda_dev))["cube"]
     torch.cuda.synchronize()
     assert rel(tuned, default) <= 1e-5

@@ -2,14 +2,21 @@
 
 What is tuned: the pixel block of a 512-pixel tile along the scan's (depth,
 lateral, elevation) axes, the order in which tiles are handed to the SMs (most
-receive channels first, or scan order), and for dimension.both the number of CTAs
-per tile (1, or 2 that each take half of the tile's stages and add their partial
-sums).  The block sets each tile's
-delay spans, hence the length of every staged sample window, how many receive
-channels are active somewhere in the tile, and how the 32 pixels of a warp
-spread over shared-memory banks; the order sets the tail of the launch.  The
-stage shape (slots per stage, samples per slot) and the CTAs per SM (one
-512-thread CTA, which the register file allows) are fixed by the kernel.
+receive channels first, or scan order), the stage shape (which (channel, wave)
+pairs share a shared-memory stage and the loop order: waves outer 2 x 16, channels
+outer 8 x 4 or 16 x 2), and for dimension.both the number of CTAs per tile (1, or 2
+that each take half of the tile's stages and add their partial sums).  The block
+sets each tile's delay spans, hence the length of every staged sample window, how
+many receive channels are active somewhere in the tile, and how the 32 pixels of a
+warp spread over shared-memory banks; the order sets the tail of the launch; the
+stage shape sets how often the receive geometry (per pixel and channel) and the
+transmit geometry (per pixel and wave) are formed, and how many of a stage's slots
+a short wave sequence fills (11 waves fill 11 of 16 slots of a waves-outer chunk,
+11 of 12 of channels-outer chunks).  Fixed by the kernel, because measurement showed
+no gain from changing them: the samples per slot (160; 104- and 80-entry slots with
+3- and 4-deep buffer rings ran at the same speed) and one 512-thread CTA per SM (the
+register file's limit); the persistent launches use one CTA per SM unless a caller
+bounds them to share the GPU with other streams (``fast.das_fast_batch(max_ctas=)``).
 
 Each candidate is timed with CUDA events on the caller's data; the fastest is
 stored under a key made of the device name and the request's shape, so later
@@ -42,6 +49,7 @@ class Choice:
     order: str                        # "cost" | "scan"
     ms: float = float("nan")          # measured time of one call (CUDA events)
     ctas_per_tile: int = 0            # dimension.both: 1 or 2 CTAs per tile, 0 = library's choice
+    stage_shape: int = 0              # 1 waves outer 2x16, 2 channels outer 8x4, 3 channels outer 16x2, 0 library's
 
 
 def cache_path() -> str:
@@ -86,13 +94,26 @@ def shape_key(scan: Scan, n_elements: int, n_waves: int, L: int, F: int, precisi
                                      L, F, int(precision), int(dimension), int(bool(is_complex))))
 
 
-def candidates(scan: Scan, both: bool = False) -> List[Choice]:
+def shapes_for(dimension) -> List[int]:
+    """Stage shapes a dimension mode runs with (ustb_das_geometry.stage_shape values)."""
+    d = int(dimension)
+    if d == 1:
+        return [1]
+    if d in (0, 2):
+        return [2, 3]
+    return [1, 2, 3]
+
+
+def candidates(scan: Scan, both: bool = False, dimension: Optional[int] = None) -> List[Choice]:
     """The planner's default block plus power-of-two blocks of 512 pixels over the
     scan's two largest axes, each in both orders; for dimension.both also the default
-    block with 1 and with 2 CTAs per tile."""
+    block with 1 and with 2 CTAs per tile; with ``dimension`` given, the default block
+    with every stage shape that mode runs with."""
     out = [Choice(None, "cost"), Choice(None, "scan")]
     if both:
         out += [Choice(None, "cost", ctas_per_tile=1), Choice(None, "cost", ctas_per_tile=2)]
+    if dimension is not None:
+        out += [Choice(None, "cost", stage_shape=sh) for sh in shapes_for(dimension)]
     g = _grid_shape(scan)
     if g is None:
         return out
@@ -112,24 +133,25 @@ def candidates(scan: Scan, both: bool = False) -> List[Choice]:
 
 def tune(make_geometry: Callable[..., "fast.FastGeometry"],
          run: Callable[["fast.FastGeometry"], None], key: str, reps: int = 3, refresh: bool = False,
-         cands: Optional[List[Choice]] = None, scan: Optional[Scan] = None, both: bool = False) -> Choice:
+         cands: Optional[List[Choice]] = None, scan: Optional[Scan] = None, both: bool = False,
+         dimension: Optional[int] = None) -> Choice:
     """Return the cached choice for ``key``, or time every candidate and cache the fastest.
 
-    ``make_geometry(block, order, ctas_per_tile)`` builds a ``FastGeometry`` with that plan;
-    ``run(geometry)`` launches the work to time on the current stream.  Candidates
-    whose plan overflows a sample window (the kernel flags it) are skipped."""
+    ``make_geometry(block, order, ctas_per_tile, stage_shape)`` builds a ``FastGeometry``
+    with that plan; ``run(geometry)`` launches the work to time on the current stream.
+    Candidates whose plan overflows a sample window (the kernel flags it) are skipped."""
     if not refresh:
         hit = _load().get(key)
         if hit is not None:
             b = hit.get("block")
             return Choice(tuple(b) if b is not None else None, hit.get("order", "cost"), hit.get("ms", float("nan")),
-                          int(hit.get("ctas_per_tile", 0)))
+                          int(hit.get("ctas_per_tile", 0)), int(hit.get("stage_shape", 0)))
     if cands is None:
-        cands = candidates(scan, both) if scan is not None else [Choice(None, "cost")]
+        cands = candidates(scan, both, dimension) if scan is not None else [Choice(None, "cost")]
     best: Optional[Choice] = None
     for c in cands:
         try:
-            geom = make_geometry(c.block, c.order, c.ctas_per_tile)
+            geom = make_geometry(c.block, c.order, c.ctas_per_tile, c.stage_shape)
         except ValueError:
             continue
         try:
@@ -147,7 +169,7 @@ def tune(make_geometry: Callable[..., "fast.FastGeometry"],
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         if best is None or ms < best.ms:
-            best = Choice(c.block, c.order, ms, c.ctas_per_tile)
+            best = Choice(c.block, c.order, ms, c.ctas_per_tile, c.stage_shape)
     if best is None:
         raise RuntimeError("no tile plan candidate ran")
     _store(key, best)
