@@ -602,6 +602,8 @@ def main():
                     help="launch only the kernels of one workload (headline, a synth.CONFIGS name, or "
                          "demod / image / coherence for the kernels around the beamformer) "
                          "--steps times each, for ncu; prints their CUDA-event times")
+    ap.add_argument("--stage-shape", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="stage shape of the fast kernel under --profile (0: the library's choice)")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "bf16"],
                     help="channel storage of the fast kernel under --profile")
     args = ap.parse_args()
@@ -948,7 +950,7 @@ def main_profile(args):
     prec = Precision[args.storage]
     cplx = ch.is_complex()
     epi = wl.epilogue is not None
-    geom = das.fast_geometry(dev)
+    geom = das.fast_geometry(dev, stage_shape=args.stage_shape)
     st = fast.convert_channels(ch, prec)
     flags = torch.zeros(1, dtype=torch.int32, device=dev)
     L = ch.shape[-1]
