@@ -167,8 +167,82 @@ __device__ __forceinline__ void chunk_units(const TableArgs& A, IDX nL, const ID
     }
 }
 
+// The index half of one channel's WC units (dimension both / receive): das_c's delay,
+// the sample index and fraction, and which units are valid.  Formed one channel
+// ahead, so that the same arithmetic also prefetches the channel's sample lines into
+// L1, and carried to the next iteration, where unit_sum adds the units.
+template <typename IDX>
+struct UnitIdx {
+    float delay[WC], b[WC];
+    IDX base[WC];
+    unsigned ok;  // bit k: unit k valid (k < wc, nonzero weights, 0 < n0 < L - 1)
+};
+
+template <bool CPLX, typename IDX, bool MAGIC>
+__device__ __forceinline__ void unit_index(const TableArgs& A, IDX nL, const IDX* wbase, int wc, const float* txd,
+                                           const float* txa, float rxd, float rxa, bool prefetch, UnitIdx<IDX>& u) {
+    const unsigned Lm2 = (unsigned)(A.L - 2);
+    u.ok = 0u;
+#pragma unroll
+    for (int k = 0; k < WC; ++k) {
+        const float delay = __fadd_rn(txd[k], rxd);
+        const float denay = __fmul_rn(__fsub_rn(delay, A.t0), A.fs);
+        float fl;
+        const int n0 = trunc_floor<MAGIC>(denay, fl);
+        const bool ok = k < wc && txa[k] != 0.0f && rxa != 0.0f && (unsigned)(n0 - 1) < Lm2;
+        u.delay[k] = delay;
+        u.b[k] = __fsub_rn(denay, fl);
+        u.base[k] = nL + wbase[k] + (IDX)(ok ? n0 : 1);
+        u.ok |= ok ? (1u << k) : 0u;
+        if (prefetch && ok) {
+            const char* x = reinterpret_cast<const char*>(A.ch) + (size_t)u.base[k] * (CPLX ? 8 : 4);
+            asm volatile("prefetch.global.L1 [%0];\n" ::"l"(x));
+        }
+    }
+}
+
+template <bool CPLX, int FC, bool PER_WAVE, typename IDX>
+__device__ __forceinline__ void unit_sum(const TableArgs& A, const UnitIdx<IDX>& u, const float* txa, float rxa,
+                                         int nf, Acc<CPLX, FC>* acc) {
+#pragma unroll
+    for (int k = 0; k < WC; ++k) {
+        const bool ok = (u.ok >> k) & 1u;
+        const float apo = __fmul_rn(txa[k], rxa);
+        const float b = u.b[k], a = __fsub_rn(1.0f, b);
+        float wr = apo, wi = 0.f;
+        if (CPLX) {
+            float c, sn;
+            ustb::expi_reduced(__fmul_rn(A.wd, u.delay[k]), c, sn);
+            wr = c * apo;
+            wi = sn * apo;
+        }
+#pragma unroll
+        for (int f = 0; f < FC; ++f) {
+            if (f >= nf) continue;
+            Acc<CPLX, FC>& ac = acc[PER_WAVE ? k : 0];
+            if (CPLX) {
+                const float2* x = reinterpret_cast<const float2*>(A.ch) + u.base[k] + f * A.LNW;
+                const float2 x0 = __ldg(x), x1 = __ldg(x + 1);
+                const float vr = fmaf(b, x1.x, a * x0.x);
+                const float vi = fmaf(b, x1.y, a * x0.y);
+                const float nr = fmaf(wr, vr, fmaf(-wi, vi, ac.re[f]));
+                const float ni = fmaf(wr, vi, fmaf(wi, vr, ac.im[f]));
+                ac.re[f] = ok ? nr : ac.re[f];
+                ac.im[f] = ok ? ni : ac.im[f];
+            } else {
+                const float* x = reinterpret_cast<const float*>(A.ch) + u.base[k] + f * A.LNW;
+                const float x0 = __ldg(x), x1 = __ldg(x + 1);
+                const float nr = fmaf(wr, fmaf(b, x1, a * x0), ac.re[f]);
+                ac.re[f] = ok ? nr : ac.re[f];
+            }
+        }
+    }
+}
+
+// Real data: at most 80 registers (6 CTAs of 128 threads per SM), with the carried unit
+// indices; complex data: the phase of every unit needs more registers.
 template <int MODE, bool CPLX, int FC, typename IDX, bool MAGIC>
-__global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) {
+__global__ void __launch_bounds__(kThreads, (CPLX ? 1 : 6)) das_table_kernel(const TableArgs A) {
     const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     if (p >= A.P) return;
     const int64_t P = A.P;
@@ -225,9 +299,32 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
                 pa += 2 * P;
                 pd += 2 * P;
                 IDX nL = (IDX)A.L * (IDX)nlo;
-                if (FC == 1 && nlo <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL, wbase, wc, txd, rxd1, rxa1);
+                if constexpr (CPLX) {
+                    // complex: a channel's unit indices are formed twice (prefetch, units),
+                    // which keeps the register count low enough for the per-unit phase
+                    if (FC == 1 && nlo <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL, wbase, wc, txd, rxd1, rxa1);
+                    for (int n = nlo; n <= nhi; ++n, nL += (IDX)A.L) {
+                        const float rxa = rxa1, rxd = rxd1;
+                        rxa1 = rxa2;
+                        rxd1 = rxd2;
+                        if (n + 2 <= nhi) {
+                            rxa2 = ld_stream(pa);
+                            rxd2 = ld_stream(pd);
+                            pa += P;
+                            pd += P;
+                        }
+                        if (FC == 1 && n + 1 <= nhi)
+                            prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
+                        if (rxa == 0.0f) continue;
+                        chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, nL, wbase, wc, f0, nf, txd, txa, rxd, rxa,
+                                                                          acc);
+                    }
+                } else {
+                // real: the indices formed with the prefetch are carried to the units
+                UnitIdx<IDX> cur, nxt;
+                if (nlo <= nhi) unit_index<CPLX, IDX, MAGIC>(A, nL, wbase, wc, txd, txa, rxd1, rxa1, FC == 1, cur);
                 for (int n = nlo; n <= nhi; ++n, nL += (IDX)A.L) {
-                    const float rxa = rxa1, rxd = rxd1;
+                    const float rxa = rxa1;
                     rxa1 = rxa2;
                     rxd1 = rxd2;
                     if (n + 2 <= nhi) {
@@ -236,9 +333,11 @@ __global__ void __launch_bounds__(kThreads) das_table_kernel(const TableArgs A) 
                         pa += P;
                         pd += P;
                     }
-                    if (FC == 1 && n + 1 <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
-                    if (rxa == 0.0f) continue;
-                    chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, nL, wbase, wc, f0, nf, txd, txa, rxd, rxa, acc);
+                    if (n + 1 <= nhi)
+                        unit_index<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, txa, rxd1, rxa1, FC == 1, nxt);
+                    if (rxa != 0.0f) unit_sum<CPLX, FC, PER_WAVE, IDX>(A, cur, txa, rxa, nf, acc);
+                    cur = nxt;
+                }
                 }
                 if (MODE == USTB_DIM_RECEIVE)
 #pragma unroll
