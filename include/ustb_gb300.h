@@ -50,7 +50,7 @@ enum { USTB_DIM_NONE = 0, USTB_DIM_RECEIVE = 1, USTB_DIM_TRANSMIT = 2, USTB_DIM_
 const char* ustb_last_error(void);
 
 /* ABI version of this library (major*10000 + minor*100 + patch). */
-int ustb_abi_version(void); /* 10200: ustb_das_geometry.stage_shape */
+int ustb_abi_version(void); /* 10300: ustb_serve_create_ex; 10200: ustb_das_geometry.stage_shape */
 
 /*
  * Plain single-precision DAS on precomputed delay/apodization tables: the
@@ -366,19 +366,27 @@ int ustb_plan_execute(ustb_plan plan, const void* ch, const ustb_das_outputs* ou
 /*
  * Continuous-batching server.  ustb_serve_submit queues one request (a plan, its
  * device channel data and outputs; both must stay valid until the request is
- * done) and returns at once with a ticket.  A scheduler thread takes queued
- * requests in arrival order into batches whose interpolation entries fit
- * `workspace_budget` bytes (at most `max_batch` requests, at most 40) and launches
- * each batch as ustb_das_fast_batch_ws, alternating between two streams of its
- * own with a workspace each; a completion thread waits for each batch and marks
- * its tickets done.  A request whose entries alone exceed the budget, or with more
- * than `large_units` pixel x channel x wave x frame units (0: 2e9), runs in a
- * batch of its own, so small requests never wait for a large one's launch.  The reference serves no requests: das.m beamforms one call
- * at a time.
+ * done) and returns at once with a ticket.  A request with more than `large_units`
+ * pixel x channel x wave x frame units (0: 2e9) is large.  A scheduler thread takes
+ * small requests in arrival order into batches whose interpolation entries fit
+ * `workspace_budget` bytes (at most `max_batch` requests, at most 40; a request
+ * whose entries alone exceed the budget runs alone) and launches each batch as
+ * ustb_das_fast_batch_ex, alternating between two streams of its own with a
+ * workspace each.  Large requests launch one per batch on a third stream (at most
+ * two queued there), so small batches never wait behind a large launch on a stream;
+ * ustb_serve_create_ex's `reserve_sms` > 0 also caps a large launch at SMs -
+ * reserve_sms persistent CTAs, keeping that many SMs for small batches while it
+ * runs (0: a large launch may use every SM, which favours throughput).  One
+ * completion thread per class (small, large) waits for its batches and marks their
+ * tickets done.  The reference serves no requests: das.m beamforms one call at a
+ * time.
  */
 typedef struct ustb_server_s* ustb_server;
 
 int ustb_serve_create(int64_t workspace_budget, int32_t max_batch, int64_t large_units, ustb_server* server);
+/* ustb_serve_create with SMs kept free of large launches (ABI 10300). */
+int ustb_serve_create_ex(int64_t workspace_budget, int32_t max_batch, int64_t large_units, int32_t reserve_sms,
+                         ustb_server* server);
 int ustb_serve_submit(ustb_server server, ustb_plan plan, const void* ch, const ustb_das_outputs* out,
                       uint64_t* ticket);
 /* Wait until the ticket's request is done (timeout_ms < 0: no limit); USTB_E_TIMEOUT

@@ -84,6 +84,7 @@ def test_plan_and_server_argument_errors_without_gpu(lib_path):
     out = ctypes.c_void_p()
     assert h.ustb_serve_create(0, 1, 0, ctypes.byref(out)) == 1 and b"budget" in h.ustb_last_error()
     assert h.ustb_serve_create(1 << 20, 41, 0, ctypes.byref(out)) == 1 and b"max_batch" in h.ustb_last_error()
+    assert h.ustb_serve_create_ex(1 << 20, 1, 0, -1, ctypes.byref(out)) == 1 and b"reserve_sms" in h.ustb_last_error()
     assert h.ustb_serve_submit(None, None, None, None, None) == 1
     assert h.ustb_serve_wait(None, 1, 0, None) == 1
     assert h.ustb_serve_destroy(None) == 1

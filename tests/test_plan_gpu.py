@@ -91,6 +91,33 @@ def test_server_batches_match_single_launches(workloads, budget):
     srv.close()
 
 
+@pytest.mark.parametrize("reserve_sms", [0, 24])
+def test_server_large_stream_matches_single_launches(workloads, reserve_sms):
+    """Requests above large_units launch alone on the large stream (capped at
+    SMs - reserve_sms CTAs) while the others batch on the small streams; each result
+    is what the request gives alone."""
+    plans = {k: make_plan(w) for k, w in workloads.items()}
+    units = {k: w["geom"].P * w["geom"].N * w["geom"].W for k, w in workloads.items()}
+    cut = sorted(units.values())[1]  # two kinds large, two small
+    srv = Server(max_batch=16, large_units=cut, reserve_sms=reserve_sms)
+    tickets = []
+    for rep in range(4):
+        for k, w in workloads.items():
+            tickets.append((k, srv.submit(plans[k], w["st"])))
+    for k, t in tickets:
+        outs = srv.wait(t)
+        assert outs["flags"] == 0
+        check(outs, workloads[k]["ref"])
+    srv.close()
+
+
+def test_server_reserve_must_leave_sms(cuda_dev):
+    sms = torch.cuda.get_device_properties(cuda_dev).multi_processor_count
+    with pytest.raises(UstbError) as e:
+        Server(reserve_sms=sms)
+    assert e.value.code == 1
+
+
 def test_server_from_several_threads(workloads):
     plans = {k: make_plan(w) for k, w in workloads.items()}
     srv = Server(max_batch=8)

@@ -45,6 +45,7 @@ SIGNATURES = {
     "ustb_plan_tiles_host": (i64, [vp, vp, i64]),
     "ustb_plan_execute": (ctypes.c_int, [vp, vp, vp, vp, vp]),
     "ustb_serve_create": (ctypes.c_int, [i64, i32, i64, vp]),
+    "ustb_serve_create_ex": (ctypes.c_int, [i64, i32, i64, i32, vp]),
     "ustb_serve_submit": (ctypes.c_int, [vp, vp, vp, vp, vp]),
     "ustb_serve_wait": (ctypes.c_int, [vp, ctypes.c_uint64, i32, vp]),
     "ustb_serve_destroy": (ctypes.c_int, [vp]),

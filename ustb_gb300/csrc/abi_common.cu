@@ -30,4 +30,4 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 
 extern "C" const char* ustb_last_error(void) { return ustb::g_last_error.c_str(); }
 
-extern "C" int ustb_abi_version(void) { return 10200; }
+extern "C" int ustb_abi_version(void) { return 10300; }

@@ -152,17 +152,20 @@ class Plan:
 
 class Server:
     """``ustb_serve_*``: queue requests on plans; the library's scheduler thread batches
-    them (entries within ``workspace_budget`` bytes, at most ``max_batch``; requests of
-    more than ``large_units`` units alone, 0 = 2e9) into persistent launches on its own
-    streams and its completion thread marks them done.
+    small requests (entries within ``workspace_budget`` bytes, at most ``max_batch``)
+    into persistent launches on two streams of its own, and launches each request of
+    more than ``large_units`` units (0 = 2e9) alone on a third stream with at most
+    SMs - ``reserve_sms`` CTAs (0: every SM); its completion threads mark them done.
     Channel data must be ready on the device when submitted (synchronize the
     producing stream first) and stays referenced until ``wait`` returns."""
 
-    def __init__(self, workspace_budget: int = 8 << 30, max_batch: int = 16, device=None, large_units: int = 0):
+    def __init__(self, workspace_budget: int = 8 << 30, max_batch: int = 16, device=None, large_units: int = 0,
+                 reserve_sms: int = 0):
         self.device = torch.device(device) if device is not None else torch.device("cuda", 0)
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.call("ustb_serve_create", int(workspace_budget), int(max_batch), int(large_units), ctypes.byref(h))
+            _lib.call("ustb_serve_create_ex", int(workspace_budget), int(max_batch), int(large_units),
+                      int(reserve_sms), ctypes.byref(h))
         self.handle = h
         self._pending: Dict[int, tuple] = {}
 
