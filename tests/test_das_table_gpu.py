@@ -135,6 +135,16 @@ def test_empty_and_degenerate_sizes(cuda_dev):
     out = kernels.das_table_f32(ch, 1.0, 0.0, t, t2, t * 0.5, t2 * 0.25, 0.0, 0)
     torch.cuda.synchronize()
     assert torch.count_nonzero(out).item() == 0
+    # L = 1 and 2, real and complex, sample positions well past the trace: no valid unit
+    for L in (1, 2):
+        for cplx in (True, False):
+            ch = torch.ones((1, 2, 3, L), dtype=torch.complex64 if cplx else torch.float32, device=dev)
+            ta = torch.ones((2, 7), dtype=torch.float32, device=dev)
+            ra = torch.ones((3, 7), dtype=torch.float32, device=dev)
+            for dim in range(4):
+                out = kernels.das_table_f32(ch, 1.0, 0.0, ta, ra, ta * 3.0, ra * 2.0, 0.0, dim)
+                torch.cuda.synchronize()
+                assert torch.count_nonzero(out).item() == 0, (L, cplx, dim)
 
 
 def test_error_codes(cuda_dev):

@@ -113,10 +113,13 @@ __device__ __forceinline__ void prefetch_units(const TableArgs& A, IDX nL, const
 }
 
 // IDX: int32_t when every sample index of the call fits 31 bits, else int64_t.
+// pf: also prefetch into L1 the next channel's sample line of each unit, at this unit's
+// sample index shifted by dn, the receive-delay step to the next channel in samples
+// (clamped into the trace; only where the lines are, not which units are valid).
 template <bool CPLX, int FC, bool PER_WAVE, int NACC, typename IDX, bool MAGIC>
 __device__ __forceinline__ void chunk_units(const TableArgs& A, IDX nL, const IDX* wbase, int wc, int64_t f0,
                                             int nf, const float* txd, const float* txa, float rxd, float rxa,
-                                            Acc<CPLX, FC>* acc) {
+                                            Acc<CPLX, FC>* acc, bool pf = false, int dn = 0) {
     float a[WC], b[WC], wr[WC], wi[WC];
     IDX base[WC];
     bool ok[WC];
@@ -129,6 +132,12 @@ __device__ __forceinline__ void chunk_units(const TableArgs& A, IDX nL, const ID
         float fl;
         const int n0 = trunc_floor<MAGIC>(denay, fl);
         ok[k] = k < wc && txa[k] != 0.0f && rxa != 0.0f && n0 > 0 && n0 < Lm1;
+        if (pf && k < wc) {
+            const int m = min(max(n0 + dn, 1), Lm1 - 1);
+            const char* x = reinterpret_cast<const char*>(A.ch) +
+                            (size_t)(nL + (IDX)A.L + wbase[k] + (IDX)m) * (CPLX ? 8 : 4);
+            asm volatile("prefetch.global.L1 [%0];\n" ::"l"(x));
+        }
         b[k] = __fsub_rn(denay, fl);
         a[k] = __fsub_rn(1.0f, b[k]);
         base[k] = nL + wbase[k] + (IDX)(ok[k] ? n0 : 1);
@@ -181,7 +190,7 @@ struct UnitIdx {
 template <bool CPLX, typename IDX, bool MAGIC>
 __device__ __forceinline__ void unit_index(const TableArgs& A, IDX nL, const IDX* wbase, int wc, const float* txd,
                                            const float* txa, float rxd, float rxa, bool prefetch, UnitIdx<IDX>& u) {
-    const unsigned Lm2 = (unsigned)(A.L - 2);
+    const unsigned Lm2 = (unsigned)(A.L - 2);  // L >= 3 here (the host zero-fills shorter traces)
     u.ok = 0u;
 #pragma unroll
     for (int k = 0; k < WC; ++k) {
@@ -300,8 +309,11 @@ __global__ void __launch_bounds__(kThreads, (CPLX ? 1 : 6)) das_table_kernel(con
                 pd += 2 * P;
                 IDX nL = (IDX)A.L * (IDX)nlo;
                 if constexpr (CPLX) {
-                    // complex: a channel's unit indices are formed twice (prefetch, units),
-                    // which keeps the register count low enough for the per-unit phase
+                    // complex: the register count left by the per-unit phase allows no
+                    // carried indices; the next channel's lines are prefetched from this
+                    // channel's indices shifted by the receive-delay step (the first
+                    // channel, and lanes without a weight on this channel, form the next
+                    // channel's indices for the prefetch)
                     if (FC == 1 && nlo <= nhi) prefetch_units<CPLX, IDX, MAGIC>(A, nL, wbase, wc, txd, rxd1, rxa1);
                     for (int n = nlo; n <= nhi; ++n, nL += (IDX)A.L) {
                         const float rxa = rxa1, rxd = rxd1;
@@ -313,11 +325,14 @@ __global__ void __launch_bounds__(kThreads, (CPLX ? 1 : 6)) das_table_kernel(con
                             pa += P;
                             pd += P;
                         }
-                        if (FC == 1 && n + 1 <= nhi)
-                            prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
-                        if (rxa == 0.0f) continue;
+                        const bool pf = FC == 1 && n + 1 <= nhi && rxa1 != 0.0f;
+                        if (rxa == 0.0f) {
+                            if (pf) prefetch_units<CPLX, IDX, MAGIC>(A, nL + (IDX)A.L, wbase, wc, txd, rxd1, rxa1);
+                            continue;
+                        }
+                        const int dn = __float2int_rn(__fmul_rn(__fsub_rn(rxd1, rxd), A.fs));
                         chunk_units<CPLX, FC, PER_WAVE, NACC, IDX, MAGIC>(A, nL, wbase, wc, f0, nf, txd, txa, rxd, rxa,
-                                                                          acc);
+                                                                          acc, pf, dn);
                     }
                 } else {
                 // real: the indices formed with the prefetch are carried to the units
@@ -496,8 +511,9 @@ extern "C" int ustb_das_table_f32(const void* ch, int32_t ch_complex, int64_t L,
     const int64_t n_out = out_elems(dimension, P, N, W, F);
     if (n_out == 0) return USTB_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (L == 0 || N == 0 || W == 0) {
-        // nothing to sum: das_c returns its zero-initialised output
+    if (L < 3 || N == 0 || W == 0) {
+        // nothing to sum (a valid unit needs 0 < n0 < L - 1): das_c returns its
+        // zero-initialised output
         USTB_CUDA(cudaMemsetAsync(out, 0, (size_t)n_out * (ch_complex ? 8 : 4), s));
         return USTB_OK;
     }
