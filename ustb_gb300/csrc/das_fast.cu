@@ -77,6 +77,7 @@ struct Params {
     uint32_t* flags;
     int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list); 0 = auto
     int shape;  // stage shape (Shape<> index)
+    int fpi;    // persistent kernel: frames per work item (one tile, consecutive frames)
 };
 
 // ---------------------------------------------------------------------------
@@ -412,8 +413,12 @@ __device__ __forceinline__ float frac_cycles(double v) { return (float)(v - floo
 // A plane or photoacoustic wave's s_tx is affine in the pixel position and a
 // spherical wave's is sigma |p - src| fs/c + const; the per-tile coefficients
 // sit in shared memory (txc, txp).
-template <int MODE, bool CPLX, bool EPI, int SHAPE>
-__device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, int half = -1) {
+//
+// FRAMES (persistent kernel): frames f_first .. f_first + nfr - 1 of the tile in turn,
+// after one build of the tile's tables and stage list (the geometry is the same for
+// every frame of a request).
+template <int MODE, bool CPLX, bool EPI, int SHAPE, bool FRAMES = false>
+__device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_first, int half = -1, int nfr = 1) {
     constexpr bool ORDER_A = Shape<SHAPE>::WAVES_OUTER;
     constexpr int CG = Shape<SHAPE>::CG;
     constexpr int KW = Shape<SHAPE>::KW;
@@ -632,6 +637,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
     __syncthreads();
     const int nstages = s_nstages;
 
+    auto frame = [&](const int64_t f) {
     const float2 ph = A.pix_phase ? __ldg(A.pix_phase + p) : make_float2(1.f, 0.f);
     const float fdfs = (float)fd_fs;
     const int64_t frame_tr = f * W * N;  // first trace of this frame
@@ -1009,7 +1015,13 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f, i
         }
     }
     cp_async_wait_all();  // only empty groups remain
-    __syncthreads();      // the buffers and per-tile tables are reused by the next tile
+    __syncthreads();      // the buffers are reused by the next frame, the tables by the next tile
+    };
+    if constexpr (FRAMES) {
+        for (int64_t f = f_first; f < f_first + nfr; ++f) frame(f);
+    } else {
+        frame(f_first);
+    }
 }
 
 // One launch per request: grid = (tiles x CTAs per tile, frames).
@@ -1022,9 +1034,11 @@ __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX>::value)) das_fast_kern
         das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
 }
 
-// Persistent form: one CTA per SM pulls (request, frame, tile) work items from a
+// Persistent form: one CTA per SM pulls (request, tile, frames) work items from a
 // queue counter until the batch is done, so requests of different scans, channel
-// counts and frame counts share one launch and balance across SMs.
+// counts and frame counts share one launch and balance across SMs.  An item is one
+// tile over up to 8 consecutive frames of a request (fewer while that leaves each CTA
+// under 8 items), so the tile's tables are built once for those frames.
 constexpr int kMaxBatch = 40;
 struct BatchParams {
     Params req[kMaxBatch];
@@ -1048,7 +1062,9 @@ __global__ void __launch_bounds__(kTile, 1) das_fast_persistent(const __grid_con
         while (r + 1 < B.n && B.first_item[r + 1] <= item) ++r;
         const Params& A = B.req[r];
         const int64_t local = item - B.first_item[r];
-        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)(local % A.n_tiles), local / A.n_tiles);
+        const int64_t f0 = (local / A.n_tiles) * A.fpi;
+        das_tile<MODE, CPLX, EPI, SHAPE, true>(A, (int)(local % A.n_tiles), f0, -1,
+                                               (int)min((int64_t)A.fpi, A.F - f0));
     }
 }
 
@@ -1105,25 +1121,28 @@ int launch_batch(const Params* reqs, const int64_t* frames, int n, unsigned long
     B.n = n;
     B.counter = counter;
     B.first_item[0] = 0;
-    size_t smem = 0;
-    for (int i = 0; i < n; ++i) {
-        B.req[i] = reqs[i];
-        B.first_item[i + 1] = B.first_item[i] + reqs[i].n_tiles * frames[i];
-        smem = std::max(smem, smem_bytes<CPLX, SHAPE>(reqs[i].N, reqs[i].W));
-    }
-    if (B.first_item[n] == 0) return USTB_OK;
     int dev = 0, optin = 0, sms = 0;
     USTB_CUDA(cudaGetDevice(&dev));
     USTB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     USTB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t nct = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
+    size_t smem = 0;
+    for (int i = 0; i < n; ++i) {
+        B.req[i] = reqs[i];
+        // frames per work item: up to 8, while every CTA keeps at least 8 items of the request
+        const int64_t fpi = std::max<int64_t>(1, std::min<int64_t>(8, reqs[i].n_tiles * frames[i] / (8 * nct)));
+        B.req[i].fpi = (int)fpi;
+        B.first_item[i + 1] = B.first_item[i] + reqs[i].n_tiles * ((frames[i] + fpi - 1) / fpi);
+        smem = std::max(smem, smem_bytes<CPLX, SHAPE>(reqs[i].N, reqs[i].W));
+    }
+    if (B.first_item[n] == 0) return USTB_OK;
     USTB_REQUIRE(smem <= (size_t)optin, USTB_E_SHAPE, "a request needs %zu bytes of shared memory per tile (limit %d)",
                  smem, optin);
     auto kern = das_fast_persistent<MODE, CPLX, EPI, SHAPE>;
     USTB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     USTB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
     // one CTA per SM, or fewer (max_ctas) to leave SMs to launches on other streams
-    const int64_t ctas = max_ctas > 0 ? std::min(max_ctas, sms) : sms;
-    const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], ctas);
+    const unsigned grid = (unsigned)std::min<int64_t>(B.first_item[n], nct);
     kern<<<grid, kTile, smem, s>>>(B);
     USTB_CUDA(cudaGetLastError());
     return USTB_OK;
@@ -1317,6 +1336,7 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
                  USTB_E_ARG, "stage_shape %d does not fit dimension %d (receive: 1; transmit/none: 2 or 3)",
                  (int)g->stage_shape, (int)dimension);
     A.shape = shape_for(dimension, g->stage_shape);
+    A.fpi = 1;
     return USTB_OK;
 }
 
