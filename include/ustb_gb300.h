@@ -201,9 +201,11 @@ typedef struct {
     int32_t rx_use_origin;       /* 0: aperture centred under each pixel; 1: at rx_origin (sector scans) */
     float rx_origin[3];
     float cf_threshold;          /* coherence factor: elements with rx apodization > this count in M */
-    int32_t ctas_per_tile;       /* dimension.both, one launch per request: 1 or 2 CTAs per tile (two
-                                    add partial sums over halves of the tile's work); 0 = the library
-                                    picks 2 when there are fewer than 4 tiles per SM */
+    int32_t ctas_per_tile;       /* dimension.both, one launch per request: 1 to 4 CTAs per tile (each
+                                    adds its partial sum over an equal part of the tile's work; with 3
+                                    or 4 the sums are added in completion order, so repeated runs may
+                                    differ in the last bits); 0 = the library picks 2 when there are
+                                    fewer than 4 tiles per SM */
     int32_t stage_shape;         /* (channel, wave) pairs per shared-memory stage and loop order:
                                     1 = waves outer, 2 channels x 16 waves (dimension.both / receive);
                                     2 = channels outer, 8 x 4; 3 = channels outer, 16 x 2

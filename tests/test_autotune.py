@@ -81,6 +81,35 @@ def test_tune_times_every_candidate_and_caches_the_stage_shape(tmp_path, monkeyp
     monkeypatch.setattr(autotune.torch.cuda, "synchronize", lambda *a: None)
     best = autotune.tune(make, run, "k3", scan=s2, both=True, dimension=3)
     assert best.stage_shape == 3 and {m[3] for m in made} >= {1, 2, 3}
+    # the best plan is then tried with 1 to 4 CTAs per tile
+    assert {m[2] for m in made if m[3] == 3} >= {1, 2, 3, 4}
     assert json.load(open(tmp_path / "t.json"))["k3"]["stage_shape"] == 3
     again = autotune.tune(lambda *a: 1 / 0, run, "k3")  # from the cache, no search
     assert again.stage_shape == 3
+
+
+def test_tune_picks_the_ctas_per_tile_after_the_other_knobs(tmp_path, monkeypatch):
+    monkeypatch.setenv("USTB_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
+    s2 = LinearScan(np.linspace(-1e-2, 1e-2, 64), np.linspace(5e-3, 5e-2, 64))
+
+    class Ev:
+        t = 0.0
+
+        def __init__(self, enable_timing=True):
+            pass
+
+        def record(self):
+            self.at = Ev.t
+
+        def elapsed_time(self, other):
+            return other.at - self.at
+
+    def run(g):  # waves outer is the best shape; 4 CTAs per tile shorten it further
+        block, order, cpt, shape = g
+        Ev.t += (1.0 if shape == 1 else 2.0) - (0.25 if cpt == 4 else 0.0)
+
+    monkeypatch.setattr(autotune.torch.cuda, "Event", Ev)
+    monkeypatch.setattr(autotune.torch.cuda, "synchronize", lambda *a: None)
+    best = autotune.tune(lambda *a: a, run, "k4", scan=s2, both=True, dimension=3)
+    assert (best.stage_shape, best.ctas_per_tile) == (1, 4)
+    assert json.load(open(tmp_path / "t.json"))["k4"]["ctas_per_tile"] == 4

@@ -53,7 +53,7 @@ def test_prebuilt_entries_give_the_single_call_result(cuda_dev):
 
 @pytest.mark.parametrize("cplx", [True, False])
 def test_two_ctas_per_tile_match_one(cuda_dev, cplx):
-    """dimension.both with 1 or 2 CTAs per tile: the same sums, added in two parts."""
+    """dimension.both with 1 to 4 CTAs per tile: the same sums, added in parts."""
     wl = synth.config_iq_cpwc(device=cuda_dev, scale=0.25) if cplx else synth.config_rf_plane_wave(device=cuda_dev,
                                                                                                    scale=0.5)
     das = DAS()
@@ -63,11 +63,12 @@ def test_two_ctas_per_tile_match_one(cuda_dev, cplx):
     st = fast.convert_channels(ch, Precision.fp32)
     L = ch.shape[-1]
     outs = {}
-    for c in (1, 2):
+    for c in (1, 2, 3, 4):
         g = das.fast_geometry(cuda_dev, ctas_per_tile=c)
         outs[c] = fast.das_fast(st, Precision.fp32, cplx, g, 3, L=L)["cube"]
     torch.cuda.synchronize()
-    rel = float((outs[1] - outs[2]).abs().norm() / outs[1].abs().norm())
-    assert rel <= 1e-6
+    for c in (2, 3, 4):
+        rel = float((outs[1] - outs[c]).abs().norm() / outs[1].abs().norm())
+        assert rel <= 1e-6, c
     again = fast.das_fast(st, Precision.fp32, cplx, das.fast_geometry(cuda_dev, ctas_per_tile=2), 3, L=L)["cube"]
     assert torch.equal(again, outs[2])  # two partial sums: fl(a + b) in either order

@@ -75,7 +75,7 @@ struct Params {
     float* o_sdmas;
     int64_t rx_f, w_f, f_f;
     uint32_t* flags;
-    int split;  // grid kernel, dimension.both: 2 CTAs per tile (halves of the stage list); 0 = auto
+    int split;  // grid kernel, dimension.both: CTAs per tile (parts of the stage list, 1-4); 0 = auto
     int shape;  // stage shape (Shape<> index)
     int fpi;    // persistent kernel: frames per work item (one tile, consecutive frames)
 };
@@ -816,10 +816,11 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
     // are copied while stage si is computed.  One barrier per stage: it makes stage
     // si's entries visible to every warp and frees the other buffer (read by stage
     // si - 1) for stage si + 1's copies.
-    // half = 0 / 1: this CTA takes the first / second half of the stage list and adds
-    // its partial sum to the (zeroed) output; -1: the whole list, plain stores
-    const int s_lo = (half == 1) ? nstages / 2 : 0;
-    const int s_hi = (half == 0) ? nstages / 2 : nstages;
+    // half = k >= 0: this CTA takes part k of A.split equal parts of the stage list and
+    // adds its partial sum to the (zeroed) output; -1: the whole list, plain stores
+    const int parts = half < 0 ? 1 : A.split;
+    const int s_lo = half < 0 ? 0 : (int)((int64_t)nstages * half / parts);
+    const int s_hi = half < 0 ? nstages : (int)((int64_t)nstages * (half + 1) / parts);
     // A ring of kRing stage buffers: the copies of the first kRing - 1 stages are
     // issued up front, then stage si waits for its own copies (older commit groups),
     // one barrier publishes them and frees stage si - 1's buffer, which takes stage
@@ -839,12 +840,13 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
         bufoff = (unsigned)(((si - s_lo) % kRing) * NS * kSlot * ES);
     };
     const float2 zero2 = make_float2(0.f, 0.f);
-    // dimension.both: the pixel's sum, plain store or (split tiles) one of two partial sums
+    // dimension.both: the pixel's sum, plain store or (split tiles) one of the partial sums
     auto store_both = [&]() {
         const float2 y = CPLX ? cmul(Y, ph) : Y;
         if (half < 0) {
             store_cube(p + A.f_f * f, y);
-        } else if (live && A.cube) {  // two partial sums per pixel: fl(a + b) in either order
+        } else if (live && A.cube) {  // partial sums: two give fl(a + b) in either order; three or
+                                      // four are added in completion order (last-bit differences)
             if constexpr (CPLX) {
                 atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].x, y.x);
                 atomicAdd(&reinterpret_cast<float2*>(A.cube)[p + A.f_f * f].y, y.y);
@@ -1028,8 +1030,9 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
 template <int MODE, bool CPLX, bool EPI, int SHAPE>
 __global__ void __launch_bounds__(kTile, (CtasPerSm<CPLX>::value)) das_fast_kernel(const Params A) {
     zero_slots<CPLX>();
-    if (MODE == USTB_DIM_BOTH && A.split == 2)
-        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)(blockIdx.x >> 1), (int64_t)blockIdx.y, (int)(blockIdx.x & 1));
+    if (MODE == USTB_DIM_BOTH && A.split >= 2)
+        das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)(blockIdx.x / A.split), (int64_t)blockIdx.y,
+                                         (int)(blockIdx.x % A.split));
     else
         das_tile<MODE, CPLX, EPI, SHAPE>(A, (int)blockIdx.x, (int64_t)blockIdx.y);
 }
@@ -1106,7 +1109,7 @@ int launch(const Params& A, int64_t n_tiles, int64_t F, cudaStream_t s) {
     Params B = A;
     if (MODE != USTB_DIM_BOTH) B.split = 1;
     else if (B.split == 0) B.split = (n_tiles * F < 4 * (int64_t)sms) ? 2 : 1;
-    if (B.split == 2 && B.cube)
+    if (B.split >= 2 && B.cube)
         USTB_CUDA(cudaMemsetAsync(B.cube, 0, (size_t)(B.P * F) * (CPLX ? 8 : 4), s));
     dim3 grid((unsigned)(n_tiles * B.split), (unsigned)F);
     kern<<<grid, kTile, smem, s>>>(B);
@@ -1328,7 +1331,7 @@ static int make_params(const void* ch, int32_t storage, int32_t is_complex, int6
     const OutStrides os = out_strides(dimension, P, N, W);
     A.rx_f = os.rx_f; A.w_f = os.w_f; A.f_f = os.f_f;
     A.flags = flags;
-    USTB_REQUIRE(g->ctas_per_tile >= 0 && g->ctas_per_tile <= 2, USTB_E_ARG, "ctas_per_tile must be 0, 1 or 2");
+    USTB_REQUIRE(g->ctas_per_tile >= 0 && g->ctas_per_tile <= 4, USTB_E_ARG, "ctas_per_tile must be 0 to 4");
     A.split = g->ctas_per_tile;  // 0: chosen at launch
     USTB_REQUIRE(g->stage_shape >= 0 && g->stage_shape <= 3, USTB_E_ARG, "stage_shape must be 0, 1, 2 or 3");
     USTB_REQUIRE(g->stage_shape == 0 || dimension == USTB_DIM_BOTH ||

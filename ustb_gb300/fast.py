@@ -349,8 +349,8 @@ class FastGeometry:
         if origin is not None:
             g.rx_origin[0], g.rx_origin[1], g.rx_origin[2] = origin.x, origin.y, origin.z
         g.cf_threshold = cf_threshold
-        if ctas_per_tile not in (0, 1, 2):
-            raise ValueError("ctas_per_tile must be 0 (library's choice), 1 or 2")
+        if ctas_per_tile not in (0, 1, 2, 3, 4):
+            raise ValueError("ctas_per_tile must be 0 (library's choice) or 1 to 4")
         g.ctas_per_tile = int(ctas_per_tile)
         self.ctas_per_tile = int(ctas_per_tile)
         if stage_shape not in (0, 1, 2, 3):
