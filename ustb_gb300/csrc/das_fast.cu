@@ -454,6 +454,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
     __shared__ float2 s_red[kTile / 32];
     __shared__ int s_nstages;
     __shared__ int s_tx_general;  // a spherical or tabulated wave, or tabulated tx apodization
+    __shared__ int s_tx_sph;      // every active wave spherical, and no tx tables
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -478,7 +479,10 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
 
     // ---- per-tile window bases, lengths, activity and delay/phase coefficients ----
     const double fd_fs = (double)A.fd / (double)A.fs;
-    if (tid == 0) s_tx_general = A.tx_apo_tab != nullptr || A.tx_delay_tab != nullptr;
+    if (tid == 0) {
+        s_tx_general = A.tx_apo_tab != nullptr || A.tx_delay_tab != nullptr;
+        s_tx_sph = !s_tx_general;
+    }
     for (int n = (int)N + tid; n < NG * CG; n += kTile) {  // padding channels: never active
         el4[n] = make_float4(0.f, 0.f, 0.f, 0.f);
         base_n[n] = 0.f;
@@ -521,6 +525,7 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
         const bool act = A.tx_apo_tab != nullptr || wv.apodization != 0.f;
         if (!ok && act) atomicOr(A.flags, USTB_FLAG_WINDOW_OVERFLOW);
         if (wv.kind == USTB_WAVE_SPHERICAL && act) s_tx_general = 1;
+        if (wv.kind != USTB_WAVE_SPHERICAL && act) s_tx_sph = 0;
         const float bw = fminf(fmaxf(base, -1.0e9f), 1.0e9f);
         base_w[w] = bw;
         len_w[w] = (int)fminf(fmaxf(ceilf(hi - base), 0.f), kHalf);
@@ -735,6 +740,11 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
     // the weight is the wave's constant apodization times the phasor; padding and
     // inactive waves carry apodization 0.  No branches.
     const bool tx_affine = !s_tx_general;
+    // Diverging and focused waves (every active wave spherical, no tables): the same
+    // arithmetic as the general setup below without its per-wave branches; padding and
+    // inactive waves carry apodization 0, and a table wave without a table has fs/c = 0
+    // there, so its s_tx is the constant term as in the general setup.
+    const bool tx_sph = s_tx_sph != 0;
     auto setup_tx_affine = [&](int w0) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) {
@@ -753,6 +763,24 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
     auto setup_tx = [&](int w0) {
         if (tx_affine) {
             setup_tx_affine(w0);
+            return;
+        }
+        if (tx_sph) {
+#pragma unroll
+            for (int k = 0; k < KW; ++k) {
+                const float4 cw = txc[w0 + k];
+                const float4 q = txp[w0 + k];
+                const float dx = px - cw.x, dy = py - cw.y, dz = pz - cw.z;
+                const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                const float sv = fmaf(pz < cw.z ? -d : d, q.z, cw.w);
+                stx[k] = fminf(fmaxf(sv, 0.f), kHalf);
+                if (CPLX) {
+                    const float2 e = phasor_cycles(fmaf(sv, fdfs, q.x));
+                    Aw[k] = make_float2(q.y * e.x, q.y * e.y);
+                } else {
+                    Aw[k] = make_float2(q.y, 0.f);
+                }
+            }
             return;
         }
 #pragma unroll
