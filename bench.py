@@ -53,7 +53,7 @@ FLOP_PER_UNIT_RF = 10
 FP32_LANES_PER_SM = 128
 # DRAM bytes (read + write) of one das_fast_kernel<both, complex, f32> launch on the
 # headline workload, from an ncu capture of `bench.py --profile headline`
-TRAFFIC_FAST_F32_HEADLINE = 211_952_896
+TRAFFIC_FAST_F32_HEADLINE = 210_949_376
 
 
 def measured_peaks():
