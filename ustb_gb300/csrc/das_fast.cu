@@ -708,38 +708,58 @@ __device__ __forceinline__ void das_tile(const Params& A, int tile, int64_t f_fi
     float2 eS = make_float2(0.f, 0.f);
     float eI = 0.f, eM = 0.f, eR = 0.f, eQ = 0.f;
 
-    // Closed-form window centred under the pixel (no table, no origin): the same
-    // arithmetic as rx_apodization, without per-channel branches; padding channels sit
-    // at the origin and are inactive, so their weight is 0.
-    const bool rx_plain = !A.rx_apo_tab && !A.rx_origin && A.rx_window != USTB_WIN_NONE;
-    auto setup_rx = [&](int n0) {
-        if (rx_plain) {
+    // Closed-form window (no table): the same arithmetic as rx_apodization without
+    // per-channel branches, centred under the pixel or, for sector scans, at the
+    // aperture origin (lateral offsets from the origin per channel, the pixel's distance
+    // to it per pixel); padding channels are inactive, so their weight is 0.
+    const bool rx_plain = !A.rx_apo_tab && A.rx_window != USTB_WIN_NONE;
+    float zo = 0.f;
+    if (A.rx_origin) {
+        const float qx = px - A.ox, qy = py - A.oy, qz = pz - A.oz;
+        zo = sqrtf(qx * qx + qy * qy + qz * qz);
+    }
+    auto setup_rx_plain = [&](int n0, auto org) {
 #pragma unroll
-            for (int c = 0; c < CG; ++c) {
-                const int n = n0 + c;
-                const float4 e4 = el4[n];
-                const float dx = px - e4.x, dy = py - e4.y, dz = pz - e4.z;
-                const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-30f);
-                const float r = r2 * rsqrtf(r2);
-                const float s = (r * A.inv_c + A.lens) * A.fs - e4.w;
-                const float xd = -dx, yd = -dy, zd = dz;
-                const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
-                const float wx = window(A, fabsf(A.fnx * __fdividef(xd, zx)));
-                const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
-                const float wy = yd == 0.f ? 1.f : window(A, fabsf(A.fny * __fdividef(yd, zy)));
-                const float apo = (live && n < N && act_n[n]) ? (yd == 0.f ? wx : wx * wy) : 0.f;
-                float2 bb;
-                if (CPLX) {
-                    const float2 e = phasor_cycles(fmaf(s, fdfs, rxph[n]));
-                    bb = make_float2(apo * e.x, apo * e.y);
-                } else {
-                    bb = make_float2(apo, 0.f);
-                }
-                srx[c] = fminf(fmaxf(s, 0.f), kHalf);  // NaN -> 0: stays inside the slot
-                B[c] = bb;
-                rxapo[c] = apo;
+        for (int c = 0; c < CG; ++c) {
+            const int n = n0 + c;
+            const float4 e4 = el4[n];
+            const float dx = px - e4.x, dy = py - e4.y, dz = pz - e4.z;
+            const float r2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-30f);
+            const float r = r2 * rsqrtf(r2);
+            const float s = (r * A.inv_c + A.lens) * A.fs - e4.w;
+            constexpr bool ORG = decltype(org)::value;
+            const float xd = ORG ? e4.x - A.ox : -dx;
+            const float yd = ORG ? e4.y - A.oy : -dy;
+            const float zd = ORG ? zo : dz;
+            const float zx = clamp_ap(zd, A.fnx, A.minx, A.maxx);
+            const float wx = window(A, fabsf(A.fnx * __fdividef(xd, zx)));
+            const float zy = clamp_ap(zd, A.fny, A.miny, A.maxy);
+            const float wy = yd == 0.f ? 1.f : window(A, fabsf(A.fny * __fdividef(yd, zy)));
+            const float apo = (live && n < N && act_n[n]) ? (yd == 0.f ? wx : wx * wy) : 0.f;
+            float2 bb;
+            if (CPLX) {
+                const float2 e = phasor_cycles(fmaf(s, fdfs, rxph[n]));
+                bb = make_float2(apo * e.x, apo * e.y);
+            } else {
+                bb = make_float2(apo, 0.f);
             }
+            srx[c] = fminf(fmaxf(s, 0.f), kHalf);  // NaN -> 0: stays inside the slot
+            B[c] = bb;
+            rxapo[c] = apo;
+        }
+    };
+    auto setup_rx = [&](int n0) {
+        // the origin form only outside dimension.both (the sector scans' transmit mode):
+        // in the dimension.both kernels a second unrolled copy cost the headline 2 %
+        if (rx_plain && !A.rx_origin) {
+            setup_rx_plain(n0, std::false_type{});
             return;
+        }
+        if constexpr (MODE != USTB_DIM_BOTH) {
+            if (rx_plain) {
+                setup_rx_plain(n0, std::true_type{});
+                return;
+            }
         }
 #pragma unroll
         for (int c = 0; c < CG; ++c) {
