@@ -65,3 +65,14 @@ def test_library_planner_rejects_non_finite_positions(what):
     n = int(_lib.lib().ustb_plan_tiles_host(ctypes.addressof(d), None, 0))
     assert n == -1  # USTB_E_ARG
     assert b"non-finite" in _lib.lib().ustb_last_error()
+
+
+def test_ctas_per_tile_range():
+    """dimension.both runs 1 to 4 CTAs per tile (0: the library's choice); more is refused."""
+    scan = LinearScan(np.linspace(-2e-3, 2e-3, 16), np.linspace(5e-3, 9e-3, 32))
+    args = (Probe.linear_array(32, 0.3e-3), scan, [Wave.plane(0.0)], 20e6, 0.0, 5e6, 1540.0, "cpu",
+            Apodization(window=Window.boxcar))
+    for c in range(5):
+        assert fast.FastGeometry(*args, ctas_per_tile=c).c.ctas_per_tile == c
+    with pytest.raises(ValueError):
+        fast.FastGeometry(*args, ctas_per_tile=5)
